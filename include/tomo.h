@@ -1,0 +1,212 @@
+/*
+ * tomo.h -- C ABI of the GB300 wave-tomography engine (libtomo.so).
+ *
+ * The reference (crogers719/Tomographic-Image-Reconstruction-Algorithms) has no
+ * library boundary: each driver is a CUDA program whose hot path is a host loop
+ * of kernel launches over compile-time sized buffers.  This header is the
+ * boundary that replaces those loops.  Every entry point below names the
+ * reference code it stands in for.
+ *
+ * Conventions
+ *   - Every call returns a tomo_status; nothing throws across the ABI and
+ *     nothing calls exit().  tomo_last_error() gives a one-line reason.
+ *   - Host pointers are caller-owned and are copied in/out during the call.
+ *     Device memory is owned by the context.  Entry points with the suffix
+ *     _device take device pointers on the context's GPU and run on the
+ *     context's stream (tomo_stream()).
+ *   - One context per host thread; a context serialises on its own stream.
+ *   - Layouts are FP32 with i (x) fastest, as in the reference
+ *     (cuda_ptr.cuh:141, index i + nx*(j + ny*(k + nz*l))):
+ *       field   f[j*nx + i]                                (nx*ny)
+ *       records rec[(g*nt + k)*n_channels + c]             (G*nt*n_channels)
+ *       per-group gradients dfg[(g*ny + j)*nx + i]         (G*nx*ny)
+ *     For the reference profile the n_channels = 4*nx record channels are the
+ *     four sensor lines side by side, c = side*nx + i with side order
+ *     bottom, right, top, left (the order generate-data.cu:202-223 writes its
+ *     four files); channels outside i in [lo+1, hi-1] are always zero.
+ */
+#ifndef TOMO_H
+#define TOMO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TOMO_ABI_VERSION 1
+
+typedef enum tomo_status {
+    TOMO_OK = 0,
+    TOMO_ERR_ARG = 1,      /* invalid argument or configuration */
+    TOMO_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+    TOMO_ERR_OOM = 3,      /* device allocation failed / plan does not fit */
+    TOMO_ERR_TIMEOUT = 4,  /* a bounded device wait ran out */
+    TOMO_ERR_DIVERGED = 5, /* epsilon rose or became NaN (tomo_run) */
+    TOMO_ERR_IO = 6,       /* file missing or malformed (CLI helpers) */
+    TOMO_ERR_STATE = 7     /* call not valid in the context's current state */
+} tomo_status;
+
+/* Physics profiles.
+ * REF: the reference's discretisation in SI units (sirt-mimo.cu:17-35,511-877):
+ *      h = 1 mm, dt = 3.3333e-7 s, c0 = 1500 m/s, one-way absorbing edges with a
+ *      corner fix-up, square transducer ring, bounding-box Gaussian-cosine
+ *      emission, four sensor lines, residual written onto the sensor lines.
+ * CFG: the same method in nondimensional units on the synthetic benchmark
+ *      workloads: h = 1, Courant number C, quadratic sponge, transducers on a
+ *      circle, point Ricker emitters, point receivers, exact discrete adjoint. */
+typedef enum tomo_profile { TOMO_PROFILE_REF = 0, TOMO_PROFILE_CFG = 1 } tomo_profile;
+
+typedef struct tomo_config {
+    int32_t nx, ny, nt;           /* grid and time steps (reference: 192, 192, 401) */
+    int32_t profile;              /* tomo_profile */
+    int32_t group_size;           /* transducers per MIMO emitter group */
+    /* REF profile: sensor lines at rows/cols ring_lo and ring_hi (0-based);
+     * transducers (1-based, as Position_Transducers) on the ring ring_lo+1 ..
+     * ring_hi+1; n_transducers = 4*(ring_hi-ring_lo).  Reference: 20, 180. */
+    int32_t ring_lo, ring_hi;
+    /* CFG profile */
+    int32_t n_transducers;        /* transducers evenly on a circle */
+    float radius;                 /* circle radius in cells, centred at (nx/2, ny/2) */
+    float courant;                /* C = c0 dt / h */
+    float cells_per_wavelength;   /* Ricker peak wavelength in cells */
+    int32_t sponge_width;         /* cells */
+    float sponge_max;             /* sigma at the outer edge; sigma(d)=max*((W-d)/W)^2 */
+    /* execution plan */
+    int32_t ckpt_interval;        /* forward slices between checkpoints; 0 = plan picks */
+    int32_t groups_per_pass;      /* P of G groups resident per sweep; 0 = plan picks */
+    int32_t device;               /* CUDA device ordinal */
+    int32_t reserved[4];
+} tomo_config;
+
+/* Update rules.  Each is the field update of one reference driver; all of them
+ * consume the per-group correlation C_g = sum_k z_g(k) * Lu_g(k). */
+typedef enum tomo_method {
+    TOMO_SIRT_CLASSIC = 0,    /* sirt-mimo.cu:858-877       f += s*mask*sum_g df_g */
+    TOMO_SIRT_SCALED = 1,     /* sirt-mimo-io.cu:774-795, sirt-iter.cu, sirt-test-weight.cu:
+                                 f += s*mask*(sum_g df_g)/G */
+    TOMO_SIRT_NORM = 2,       /* sirt-mimo-norm.cu:56-118,873-892  inverse-deviation weights */
+    TOMO_SIRT_WEIGHT = 3,     /* sirt-mimo-weight.cu:786-839  mean of intermediate fields */
+    TOMO_SIRT_AVG = 4,        /* sirt-mimo-avg.cu  same, fixed scale */
+    TOMO_SIRT_AVG_WEIGHT = 5, /* sirt-mimo-avg-weight.cu:130-203  unnormalised weighted sum */
+    TOMO_ART = 6,             /* art-mimo.cu:683-736  sequential (Kaczmarz) over groups */
+    TOMO_METHOD_COUNT = 7
+} tomo_method;
+
+/* Step-size schedules, s(it) for 0-based iteration it. */
+typedef enum tomo_sched_kind {
+    TOMO_SCHED_CONST = 0,  /* s = omega                          (sirt-mimo.cu, art-mimo.cu) */
+    TOMO_SCHED_POWER = 1,  /* s = omega*(alpha + beta/(it+1)^gamma)   (sirt-mimo-norm.cu:450) */
+    TOMO_SCHED_LINEAR = 2  /* s = omega*(alpha + beta*(it+1))          (sirt-iter.cu:678) */
+} tomo_sched_kind;
+
+typedef struct tomo_schedule {
+    int32_t kind;          /* tomo_sched_kind */
+    float omega, alpha, beta, gamma;
+    int32_t normalize;     /* 1: scale the update direction by 1/max|dir| over the mask */
+    int32_t reserved[2];
+} tomo_schedule;
+
+typedef struct tomo_iter_stats {
+    double epsilon;        /* 100*||f - f_true||/||f_true|| (NaN without f_true) */
+    double resid_norm2;    /* sum of squared record residuals at the start of the iteration */
+    double scale;          /* step size used */
+    double seconds;        /* device time of the iteration */
+    double cell_updates;   /* forward + adjoint cell-updates credited (no recompute) */
+} tomo_iter_stats;
+
+typedef struct tomo_info {
+    int32_t n_groups;        /* G */
+    int32_t n_channels;      /* record channels per group and time step */
+    int32_t n_transducers;
+    int32_t groups_per_pass; /* P chosen by the plan */
+    int32_t ckpt_interval;   /* K chosen by the plan (>= nt-2: full history) */
+    int32_t n_segments;
+    int64_t device_bytes;    /* device memory held by the context */
+} tomo_info;
+
+typedef struct tomo_noise {
+    int32_t kind;            /* 0 none, 1 Gaussian rec += level*std(trace)*N(0,1) */
+    float level;
+    uint64_t seed;
+} tomo_noise;
+
+typedef struct tomo_ctx tomo_ctx;
+
+/* ---- library ---------------------------------------------------------- */
+int32_t     tomo_abi_version(void);
+const char* tomo_status_string(tomo_status s);
+/* Fill *cfg with the reference problem (profile REF: 192^2, nt 401, ring 20/180,
+ * group size 10; sirt-mimo.cu:17-35) or the 128^2 synthetic workload (CFG). */
+tomo_status tomo_config_init(tomo_config* cfg, int32_t profile);
+
+/* ---- context (replaces the device_ptr set-up in Ultrasonic_Tomography,
+ *      e.g. sirt-mimo-norm.cu:161-303) ------------------------------------ */
+tomo_status tomo_create(const tomo_config* cfg, tomo_ctx** out);
+void        tomo_destroy(tomo_ctx* ctx);
+const char* tomo_last_error(const tomo_ctx* ctx);
+tomo_status tomo_get_info(const tomo_ctx* ctx, tomo_info* out);
+void*       tomo_stream(const tomo_ctx* ctx); /* cudaStream_t of the context */
+
+/* Transducer cells.  REF: 1-based (ii, jj) exactly as Position_Transducers
+ * (sirt-mimo.cu:438-466).  CFG: 0-based cell coordinates on the circle. */
+tomo_status tomo_transducers(const tomo_ctx* ctx, int32_t* ii, int32_t* jj);
+
+/* generate-field (generate-field.cu:117-172): the reference phantom of a 30 mm
+ * disc (0.03) with three 10 mm discs (0.05) on x = -0.1 + i*h. */
+tomo_status tomo_phantom_ref(int32_t nx, int32_t ny, float* fo);
+/* Seeded synthetic phantom: kind 0 = n discs (radius U[rmin,rmax], value
+ * U[-vmax,vmax]); kind 1 = n ellipses (axes U[rmin,rmax], value U[-vmax,vmax])
+ * plus Gaussian-smoothed N(0, noise_sigma^2) texture inside the circle of
+ * radius `support`. */
+tomo_status tomo_phantom_cfg(int32_t nx, int32_t ny, int32_t kind, int32_t n,
+                             float rmin, float rmax, float vmax, float noise_sigma,
+                             float support, uint64_t seed, float* fo);
+
+/* ---- hot path ----------------------------------------------------------- */
+/* Forward solve of every group and sensor recording.  Replaces the
+ * propagation / propagation_at_corners / initial_signal launches
+ * (generate-data.cu:157-185).  records: G*nt*n_channels.  u_last (optional):
+ * G*nx*ny wavefields at the last time step nt-1. */
+tomo_status tomo_forward(tomo_ctx* ctx, const float* f, float* records, float* u_last);
+/* generate-data: forward solve plus optional seeded noise on the records. */
+tomo_status tomo_generate_data(tomo_ctx* ctx, const float* f_true, float* records,
+                               const tomo_noise* noise);
+/* Store measured records on the device for later tomo_iterate calls. */
+tomo_status tomo_set_records(tomo_ctx* ctx, const float* records);
+/* Gradient of one SIRT sweep: forward, residual, time-reversed adjoint and
+ * the correlation (sirt-mimo-norm.cu:418-439).  Outputs (each optional):
+ * dfg = per-group df_g = C_g * scale / (1 + f) (G*nx*ny), df = sum_g df_g,
+ * resid_norm2 = sum of squared record residuals. */
+tomo_status tomo_gradient(tomo_ctx* ctx, const float* f, const float* records,
+                          float* dfg, float* df, double* resid_norm2);
+/* One iteration of `method` from 0-based iteration `iter` (the body of the
+ * reference drivers' iteration loops, e.g. sirt-mimo.cu:305-370).
+ * records may be NULL to use tomo_set_records data.  f_true may be NULL. */
+tomo_status tomo_iterate(tomo_ctx* ctx, int32_t method, const tomo_schedule* sched,
+                         int32_t iter, float* f_inout, const float* records,
+                         const float* f_true, tomo_iter_stats* stats);
+/* Iterate with the reference stopping rule (sirt-mimo.cu:355-366): stop when
+ * epsilon <= target_epsilon, when epsilon rises above the previous iteration's
+ * or is NaN, or after max_iters (-1: unbounded, sirt-mimo.cu:79-80).  Needs
+ * f_true.  eps_log (optional, max_iters entries when max_iters > 0) receives
+ * epsilon per iteration; *iters_done the number of iterations run.  Returns
+ * TOMO_OK when the target was reached or the iteration budget ran out and
+ * TOMO_ERR_DIVERGED when the divergence rule stopped the loop. */
+tomo_status tomo_run(tomo_ctx* ctx, int32_t method, const tomo_schedule* sched,
+                     float* f_inout, const float* records, const float* f_true,
+                     float target_epsilon, int32_t max_iters, double* eps_log,
+                     int32_t* iters_done);
+
+/* Device-resident variants: pointers live on the context's GPU. */
+tomo_status tomo_forward_device(tomo_ctx* ctx, const float* d_f, float* d_records);
+tomo_status tomo_iterate_device(tomo_ctx* ctx, int32_t method, const tomo_schedule* sched,
+                                int32_t iter, float* d_f, const float* d_records,
+                                const float* d_f_true, tomo_iter_stats* stats);
+tomo_status tomo_synchronize(tomo_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TOMO_H */

@@ -1,0 +1,92 @@
+"""C ABI checks that need no GPU.
+
+libtomo.so builds, loads and exports every function declared in
+include/tomo.h; host-side entry points (config defaults, phantoms, argument
+validation) work without a device; with no device, tomo_create fails with a
+status instead of crashing.  The CLI writes the reference's fo.txt format.
+"""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+import tomo
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "tomo.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tomo_[a-z_]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(built_lib):
+    names = declared_functions()
+    assert len(names) >= 18
+    out = subprocess.run(["nm", "-D", "--defined-only", tomo.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (tomo_\w+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        getattr(built_lib, n)
+
+
+def test_config_defaults(built_lib):
+    c = tomo.Config()
+    assert built_lib.tomo_config_init(C.byref(c), tomo.PROFILE_REF) == 0
+    assert (c.nx, c.ny, c.nt, c.group_size, c.ring_lo, c.ring_hi) == (192, 192, 401, 10, 20, 180)
+    assert built_lib.tomo_config_init(C.byref(c), tomo.PROFILE_CFG) == 0
+    assert (c.nx, c.nt, c.n_transducers, c.group_size) == (128, 600, 32, 4)
+    assert built_lib.tomo_config_init(C.byref(c), 7) == tomo.ERR_ARG
+    assert built_lib.tomo_abi_version() == 1
+    assert built_lib.tomo_status_string(tomo.ERR_OOM) == b"out of device memory"
+
+
+def test_phantom_matches_oracle(built_lib):
+    assert np.array_equal(tomo.phantom_ref(), O.phantom_ref())
+    a = tomo.phantom_cfg(128, 128, 0, 3, 5, 15, 0.1, 0.0, 45.0, 1000)
+    b = tomo.phantom_cfg(128, 128, 0, 3, 5, 15, 0.1, 0.0, 45.0, 1000)
+    assert np.array_equal(a, b) and np.abs(a).max() <= 0.3 and (a != 0).sum() > 100
+    e = tomo.phantom_cfg(256, 256, 1, 8, 10, 60, 0.15, 0.01, 110.0, 7)
+    assert e.std() > 0.005
+
+
+def test_bad_config_rejected_before_device(built_lib):
+    for bad in (tomo.ref_config(ring_lo=1), tomo.ref_config(ring_hi=190), tomo.ref_config(group_size=0),
+                tomo.cfg_config(radius=70.0), tomo.cfg_config(courant=0.9)):
+        h = C.c_void_p()
+        st = built_lib.tomo_create(C.byref(bad), C.byref(h))
+        assert st == tomo.ERR_ARG and not h.value
+        assert built_lib.tomo_last_error(None)
+
+
+def test_create_without_gpu_is_a_status(built_lib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    st = built_lib.tomo_create(C.byref(tomo.ref_config()), C.byref(h))
+    assert st == tomo.ERR_CUDA and not h.value
+
+
+def test_cli_generate_field(built_lib, tmp_path):
+    exe = os.path.join(os.path.dirname(tomo.LIB_PATH), "..", "bin", "generate-field")
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    vals = np.array(open(tmp_path / "fo.txt").read().split(), np.float32)
+    assert np.array_equal(vals.reshape(192, 192), O.phantom_ref())
+    lines = open(tmp_path / "fo.txt").read().split("\n")
+    assert len(lines[0].split()) == 192 and lines[192] == ""
+
+
+def test_cli_usage_errors(built_lib, tmp_path):
+    exe = os.path.join(os.path.dirname(tomo.LIB_PATH), "..", "bin", "sirt-mimo-norm")
+    r = subprocess.run([exe, "fo.txt"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage" in r.stderr

@@ -1,0 +1,736 @@
+// engine.cu -- the tomo_ctx: device buffers, memory plan, checkpoint/recompute
+// schedule, CUDA-graph capture of the per-time-step launches, and the C ABI.
+//
+// The reference runs each iteration as a host loop of ~1200 launches over
+// full-history buffers u(NX,NY,NT,Ng), z(NX,NY,NT+1,Ng) and Lu(NX,NY,NT,Ng)
+// (sirt-mimo-norm.cu:259-297,407-489).  Here one iteration is:
+//   coef(f) -> per pass of P groups: [forward sweep: one launch per step for all
+//   P groups, sensor gather with residual, checkpoint stores] [adjoint sweep:
+//   per chunk of K slices (last chunk first): restore checkpoint, recompute the
+//   chunk's forward slices, adjoint steps with fused injection + correlation]
+//   -> update rule (deterministic FP64 reductions).
+// Each pass's launch sequence is captured once into a CUDA graph and replayed.
+// Without checkpointing (K >= nt-2) the whole forward history stays resident
+// and nothing is recomputed; with it, memory per group is (K+1 + 2*chunks)
+// slices instead of nt (the on-device version of the reference's
+// P-of-M-resident-groups strategy, sirt-mimo-norm-mem.cu:419-468).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "internal.h"
+
+using namespace tomo;
+
+namespace {
+thread_local std::string g_create_error;
+}
+
+struct tomo_ctx {
+    Geometry geo;
+    DevGeo dg{};
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    // plan
+    int P = 1;       // groups per pass
+    int S = 3;       // forward slots per group
+    int K = 0;       // slices per chunk
+    int nchunk = 1;
+    bool full = true;
+    // device buffers
+    float *f = nullptr, *ftrue = nullptr, *coef = nullptr, *rcoef = nullptr, *dir = nullptr, *tmp = nullptr;
+    float *hist = nullptr, *z = nullptr, *ckpt = nullptr, *corr = nullptr, *meas = nullptr, *rr = nullptr,
+          *rec = nullptr, *dfg = nullptr;
+    double *rpart = nullptr, *part = nullptr, *sums = nullptr;
+    unsigned int* maxabs = nullptr;
+    int32_t *box = nullptr, *emit = nullptr, *rcv = nullptr, *rid = nullptr;
+    float* src = nullptr;
+    uint8_t* mask = nullptr;
+    int64_t bytes = 0;
+    bool meas_set = false;
+    std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+    std::vector<void*> allocs;
+
+    tomo_status fail(tomo_status s, const char* fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return s;
+    }
+    tomo_status cuda(cudaError_t e, const char* what) {
+        if (e == cudaSuccess) return TOMO_OK;
+        if (e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            return fail(TOMO_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+        }
+        return fail(TOMO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+    template <typename T>
+    tomo_status alloc(T** p, int64_t n, const char* what) {
+        void* q = nullptr;
+        const size_t b = (size_t)std::max<int64_t>(n, 1) * sizeof(T);
+        const cudaError_t e = cudaMalloc(&q, b);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(TOMO_ERR_OOM, "cudaMalloc(%s, %zu bytes): %s", what, b, cudaGetErrorString(e));
+        }
+        allocs.push_back(q);
+        bytes += (int64_t)b;
+        *p = (T*)q;
+        return TOMO_OK;
+    }
+    ~tomo_ctx() {
+        if (dev >= 0) cudaSetDevice(dev);
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        for (void* p : allocs) cudaFree(p);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    int64_t N() const { return geo.N; }
+    int64_t slot(int k) const { return (int64_t)(k % S) * geo.N; }
+    int64_t recs_per_group() const { return (int64_t)geo.nt * geo.nch; }
+};
+
+#define TRY(x)                                   \
+    do {                                         \
+        const tomo_status _s = (x);              \
+        if (_s != TOMO_OK) return _s;            \
+    } while (0)
+#define CU(ctx, x) TRY((ctx)->cuda((x), #x))
+
+namespace {
+
+enum Mode { MODE_FWD = 0, MODE_GRAD = 1 };
+
+// Chosen memory plan.
+tomo_status make_plan(tomo_ctx* c) {
+    const Geometry& g = c->geo;
+    const int64_t N = g.N, nt = g.nt, G = g.G;
+    size_t free_b = 0, total_b = 0;
+    CU(c, cudaMemGetInfo(&free_b, &total_b));
+    // fixed buffers (fields, coefficients, accumulators, records)
+    const int64_t fixed = 4 * (6 * N) + 4 * (2 * G * N) + 4 * (2 * G * nt * g.nch) + 8 * (G * nt) +
+                          8 * (int64_t)(G + 2) * reduce_blocks() + (int64_t)(64 << 20);
+    const double budget = 0.90 * (double)free_b - (double)fixed;
+    auto per_group = [&](bool full, int K) -> double {
+        const int64_t slots = full ? nt : (int64_t)K + 1;
+        const int64_t chunks = full ? 0 : (nt - 2 + K - 1) / K;
+        return 4.0 * ((double)(slots + 3 + 2 * chunks) * N + (double)nt * g.nch);
+    };
+    int P = g.cfg.groups_per_pass > 0 ? std::min(g.cfg.groups_per_pass, g.G) : g.G;
+    int K = g.cfg.ckpt_interval;
+    bool full;
+    if (K > 0) {
+        full = K >= nt - 2;
+    } else {
+        full = per_group(true, 0) * P <= budget;
+        if (!full) K = std::max(2, (int)std::ceil(std::sqrt(2.0 * (double)(nt - 2))));
+    }
+    if (!full && K < 2) return c->fail(TOMO_ERR_ARG, "ckpt_interval must be >= 2");
+    if (g.cfg.groups_per_pass <= 0) {
+        while (P > 1 && per_group(full, K) * P > budget) --P;
+    }
+    if (per_group(full, K) * P > budget)
+        return c->fail(TOMO_ERR_OOM, "plan needs %.2f GB for %d groups per pass, %.2f GB available",
+                       per_group(full, K) * P / 1e9, P, budget / 1e9);
+    c->P = P;
+    c->full = full;
+    if (full) {
+        c->K = (int)(nt - 2);
+        c->S = (int)nt;
+        c->nchunk = 1;
+    } else {
+        c->K = K;
+        c->S = K + 1;
+        c->nchunk = (int)((nt - 2 + K - 1) / K);
+    }
+    return TOMO_OK;
+}
+
+tomo_status create_buffers(tomo_ctx* c) {
+    const Geometry& g = c->geo;
+    const int64_t N = g.N, nt = g.nt, G = g.G, P = c->P, nch = g.nch;
+    TRY(c->alloc(&c->f, N, "f"));
+    TRY(c->alloc(&c->ftrue, N, "f_true"));
+    TRY(c->alloc(&c->coef, N, "coef"));
+    TRY(c->alloc(&c->rcoef, N, "rcoef"));
+    TRY(c->alloc(&c->dir, N, "dir"));
+    TRY(c->alloc(&c->tmp, N, "tmp"));
+    TRY(c->alloc(&c->hist, P * c->S * N, "forward slots"));
+    TRY(c->alloc(&c->z, P * 3 * N, "adjoint slots"));
+    if (!c->full) TRY(c->alloc(&c->ckpt, P * c->nchunk * 2 * N, "checkpoints"));
+    TRY(c->alloc(&c->corr, G * N, "correlation"));
+    TRY(c->alloc(&c->meas, G * nt * nch, "measured records"));
+    TRY(c->alloc(&c->rr, P * nt * nch, "residual records"));
+    TRY(c->alloc(&c->rpart, G * nt, "residual partials"));
+    TRY(c->alloc(&c->part, (G + 2) * (int64_t)reduce_blocks(), "reduction partials"));
+    TRY(c->alloc(&c->sums, G + 8, "sums"));
+    TRY(c->alloc(&c->maxabs, 1, "maxabs"));
+    TRY(c->alloc(&c->mask, N, "mask"));
+    TRY(c->alloc(&c->src, nt, "source"));
+    TRY(c->alloc(&c->rcv, nch, "receivers"));
+    if (g.ref) TRY(c->alloc(&c->box, 4 * G, "boxes"));
+    else {
+        TRY(c->alloc(&c->emit, G * g.gs, "emitters"));
+        TRY(c->alloc(&c->rid, N, "receiver map"));
+    }
+    CU(c, cudaMemsetAsync(c->rr, 0, sizeof(float) * P * nt * nch, c->st));
+    CU(c, cudaMemsetAsync(c->meas, 0, sizeof(float) * G * nt * nch, c->st));
+    CU(c, cudaMemsetAsync(c->rpart, 0, sizeof(double) * G * nt, c->st));
+    CU(c, cudaMemsetAsync(c->f, 0, sizeof(float) * N, c->st));
+    CU(c, cudaMemcpyAsync(c->mask, g.mask.data(), N, cudaMemcpyHostToDevice, c->st));
+    CU(c, cudaMemcpyAsync(c->src, g.src.data(), sizeof(float) * nt, cudaMemcpyHostToDevice, c->st));
+    CU(c, cudaMemcpyAsync(c->rcv, g.rcv.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, c->st));
+    if (g.ref) CU(c, cudaMemcpyAsync(c->box, g.box.data(), sizeof(int32_t) * 4 * G, cudaMemcpyHostToDevice, c->st));
+    else {
+        CU(c, cudaMemcpyAsync(c->emit, g.emit.data(), sizeof(int32_t) * G * g.gs, cudaMemcpyHostToDevice, c->st));
+        CU(c, cudaMemcpyAsync(c->rid, g.rid.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, c->st));
+    }
+    CU(c, cudaStreamSynchronize(c->st));
+    DevGeo& d = c->dg;
+    d.nx = g.nx; d.ny = g.ny; d.nt = g.nt; d.nch = g.nch;
+    d.lo = g.lo; d.hi = g.hi; d.gs = g.gs;
+    d.sponge_w = g.cfg.sponge_width; d.sponge_max = g.cfg.sponge_max;
+    d.box = c->box; d.emit = c->emit; d.rcv = c->rcv; d.rid = c->rid; d.src = c->src;
+    d.n_src_steps = g.n_src_steps;
+    return TOMO_OK;
+}
+
+// Records the launch sequence of one pass (groups g0 .. g0+ng-1) on the stream.
+void record_pass(tomo_ctx* c, int mode, int g0, int ng) {
+    const Geometry& g = c->geo;
+    const int nt = g.nt, S = c->S, K = c->K;
+    const int64_t N = g.N, gstride = (int64_t)S * N, nch = g.nch, rpg = c->recs_per_group();
+    void* st = c->st;
+    const int prof = g.cfg.profile;
+    // ---- forward sweep
+    launch_zero_slots(c->hist, ng, gstride, c->slot(0), c->slot(1), N, st);
+    for (int k = 1; k <= nt - 2; ++k) {
+        FwdStep fs{};
+        fs.up = c->hist + c->slot(k - 1);
+        fs.uc = c->hist + c->slot(k);
+        fs.un = c->hist + c->slot(k + 1);
+        fs.gstride = gstride;
+        fs.k = k;
+        fs.g0 = g0;
+        fs.ng = ng;
+        const int m = k + 1;
+        if (mode == MODE_GRAD && !c->full) {
+            // chunk ch >= 1 starts at qa = 1 + ch*K and keeps slices qa-1 and qa.
+            int ch = -1, which = 0;
+            if (m % K == 0) { ch = m / K; which = 0; }
+            else if ((m - 1) % K == 0) { ch = (m - 1) / K; which = 1; }
+            if (ch >= 1 && ch < c->nchunk) {
+                fs.ck = c->ckpt + ((int64_t)ch * 2 + which) * N;
+                fs.ckstride = (int64_t)c->nchunk * 2 * N;
+            }
+        }
+        launch_fwd_step(prof, c->dg, c->coef, c->rcoef, fs, st);
+        GatherStep gs{};
+        gs.u = c->hist + c->slot(m);
+        gs.gstride = gstride;
+        gs.k = m;
+        gs.ng = ng;
+        if (mode == MODE_GRAD) {
+            gs.meas = c->meas + (int64_t)g0 * rpg;
+            gs.out = c->rr;
+            gs.part = c->rpart + (int64_t)g0 * nt;
+        } else {
+            gs.out = c->rec + (int64_t)g0 * rpg;
+        }
+        launch_gather(c->dg, gs, st);
+    }
+    if (mode == MODE_FWD) return;
+    // ---- adjoint sweep, chunks in reverse
+    cudaMemsetAsync(c->z, 0, sizeof(float) * 3 * N * ng, (cudaStream_t)st);
+    cudaMemsetAsync(c->corr + (int64_t)g0 * N, 0, sizeof(float) * N * ng, (cudaStream_t)st);
+    for (int ch = c->nchunk - 1; ch >= 0; --ch) {
+        const int qa = 1 + ch * K, qb = std::min(qa + K - 1, nt - 2);
+        if (!c->full) {
+            const bool in_ring = (ch == c->nchunk - 1) && (qa - 1 >= nt - S);
+            if (!in_ring) {
+                if (ch == 0) {
+                    launch_zero_slots(c->hist, ng, gstride, c->slot(qa - 1), c->slot(qa), N, st);
+                } else {
+                    const int64_t cks = (int64_t)c->nchunk * 2 * N;
+                    launch_copy_groups(c->hist + c->slot(qa - 1), gstride, c->ckpt + ((int64_t)ch * 2 + 0) * N, cks,
+                                       ng, N, st);
+                    launch_copy_groups(c->hist + c->slot(qa), gstride, c->ckpt + ((int64_t)ch * 2 + 1) * N, cks, ng,
+                                       N, st);
+                }
+                for (int m = qa + 1; m <= qb; ++m) {
+                    FwdStep fs{};
+                    fs.up = c->hist + c->slot(m - 2);
+                    fs.uc = c->hist + c->slot(m - 1);
+                    fs.un = c->hist + c->slot(m);
+                    fs.gstride = gstride;
+                    fs.k = m - 1;
+                    fs.g0 = g0;
+                    fs.ng = ng;
+                    launch_fwd_step(prof, c->dg, c->coef, c->rcoef, fs, st);
+                }
+            }
+        }
+        for (int q = qb; q >= qa; --q) {
+            const int kz = (prof == TOMO_PROFILE_REF) ? q : q + 1;
+            AdjStep as{};
+            as.z2 = c->z + (int64_t)((kz + 2) % 3) * N;
+            as.z1 = c->z + (int64_t)((kz + 1) % 3) * N;
+            as.zk = c->z + (int64_t)(kz % 3) * N;
+            as.zstride = 3 * N;
+            as.uq = c->hist + c->slot(q);
+            as.ustride = gstride;
+            as.rr = c->rr + (int64_t)kz * nch;
+            as.rrstride = rpg;
+            as.corr = c->corr + (int64_t)g0 * N;
+            as.cstride = N;
+            as.k = kz;
+            as.ng = ng;
+            launch_adj_step(prof, c->dg, c->coef, as, st);
+        }
+    }
+}
+
+tomo_status run_pass(tomo_ctx* c, int mode, int g0, int ng) {
+    const auto key = std::make_tuple(mode, g0, ng);
+    auto it = c->graphs.find(key);
+    if (it == c->graphs.end()) {
+        cudaGraph_t graph = nullptr;
+        CU(c, cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+        record_pass(c, mode, g0, ng);
+        const cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+        if (e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return c->cuda(e, "cudaStreamEndCapture");
+        }
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t e2 = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e2 != cudaSuccess) return c->cuda(e2, "cudaGraphInstantiate");
+        it = c->graphs.emplace(key, exec).first;
+    }
+    CU(c, cudaGraphLaunch(it->second, c->st));
+    return TOMO_OK;
+}
+
+tomo_status ensure_rec(tomo_ctx* c) {
+    if (!c->rec) TRY(c->alloc(&c->rec, (int64_t)c->geo.G * c->recs_per_group(), "simulated records"));
+    return TOMO_OK;
+}
+
+// Forward sweep of every group into c->rec.
+tomo_status forward_all(tomo_ctx* c, float* u_last_host) {
+    TRY(ensure_rec(c));
+    const Geometry& g = c->geo;
+    CU(c, cudaMemsetAsync(c->rec, 0, sizeof(float) * (size_t)g.G * c->recs_per_group(), c->st));
+    launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
+    for (int g0 = 0; g0 < g.G; g0 += c->P) {
+        const int ng = std::min(c->P, g.G - g0);
+        TRY(run_pass(c, MODE_FWD, g0, ng));
+        if (u_last_host)
+            for (int gl = 0; gl < ng; ++gl)
+                CU(c, cudaMemcpyAsync(u_last_host + (int64_t)(g0 + gl) * g.N,
+                                      c->hist + (int64_t)gl * c->S * g.N + c->slot(g.nt - 1), sizeof(float) * g.N,
+                                      cudaMemcpyDeviceToHost, c->st));
+    }
+    return TOMO_OK;
+}
+
+// Correlations of all groups for the current c->f (SIRT), residual partials.
+tomo_status gradient_all(tomo_ctx* c) {
+    const Geometry& g = c->geo;
+    launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
+    for (int g0 = 0; g0 < g.G; g0 += c->P) TRY(run_pass(c, MODE_GRAD, g0, std::min(c->P, g.G - g0)));
+    return TOMO_OK;
+}
+
+double sched_scale(const tomo_schedule* s, int it) {
+    switch (s->kind) {
+    case TOMO_SCHED_CONST: return s->omega;
+    case TOMO_SCHED_POWER: return (double)s->omega * ((double)s->alpha + (double)s->beta / std::pow((double)(it + 1), (double)s->gamma));
+    case TOMO_SCHED_LINEAR: return (double)s->omega * ((double)s->alpha + (double)s->beta * (double)(it + 1));
+    default: return std::numeric_limits<double>::quiet_NaN();
+    }
+}
+
+tomo_status apply_dir(tomo_ctx* c, const tomo_schedule* s, double scale) {
+    const unsigned int* mx = nullptr;
+    if (s->normalize) {
+        launch_maxabs(c->dir, c->mask, c->geo.N, c->maxabs, c->st);
+        mx = c->maxabs;
+    }
+    launch_apply(c->f, c->dir, c->mask, c->geo.N, scale, mx, c->st);
+    return TOMO_OK;
+}
+
+// Sum of the residual partials of all groups -> host.
+tomo_status residual_norm(tomo_ctx* c, double* out) {
+    const Geometry& g = c->geo;
+    launch_sum_parts(c->rpart, 1, g.G * g.nt, c->sums, c->st);
+    CU(c, cudaMemcpyAsync(out, c->sums, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    return TOMO_OK;
+}
+
+tomo_status epsilon(tomo_ctx* c, double* out) {
+    const int nb = reduce_blocks();
+    launch_eps_parts(c->f, c->ftrue, c->geo.N, c->part, nb, c->st);
+    launch_sum_parts(c->part, 2, nb, c->sums + 2, c->st);
+    double ab[2];
+    CU(c, cudaMemcpyAsync(ab, c->sums + 2, sizeof ab, cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    *out = 100.0 * std::sqrt(ab[0]) / std::sqrt(ab[1]);
+    return TOMO_OK;
+}
+
+// One iteration on c->f with c->meas; f_true in c->ftrue when have_true.
+tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int it, bool have_true,
+                         tomo_iter_stats* stats) {
+    const Geometry& g = c->geo;
+    const int64_t N = g.N;
+    const int G = g.G;
+    if (method < 0 || method >= TOMO_METHOD_COUNT) return c->fail(TOMO_ERR_ARG, "unknown method %d", method);
+    if (!sch) return c->fail(TOMO_ERR_ARG, "schedule is NULL");
+    const double s = sched_scale(sch, it);
+    if (!std::isfinite(s)) return c->fail(TOMO_ERR_ARG, "bad schedule");
+    const double sc = g.corr_scale;
+    const int nb = reduce_blocks();
+    CU(c, cudaEventRecord(c->ev0, c->st));
+    double r2 = 0.0;
+    if (method == TOMO_ART) {
+        // art-mimo.cu:688-736: each group sees the field updated by the previous one.
+        double acc = 0.0;
+        for (int gg = 0; gg < G; ++gg) {
+            launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
+            TRY(run_pass(c, MODE_GRAD, gg, 1));
+            launch_combine(c->corr + (int64_t)gg * N, 1, N, c->f, sc, nullptr, 1.0, c->dir, c->st);
+            TRY(apply_dir(c, sch, s));
+        }
+        TRY(residual_norm(c, &acc));
+        CU(c, cudaStreamSynchronize(c->st));
+        r2 = acc;
+    } else {
+        TRY(gradient_all(c));
+        TRY(residual_norm(c, &r2));
+        switch (method) {
+        case TOMO_SIRT_CLASSIC:
+            launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0, c->dir, c->st);
+            TRY(apply_dir(c, sch, s));
+            break;
+        case TOMO_SIRT_SCALED:
+        case TOMO_SIRT_WEIGHT:
+        case TOMO_SIRT_AVG:
+            launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->dir, c->st);
+            TRY(apply_dir(c, sch, s));
+            break;
+        case TOMO_SIRT_NORM: {
+            // mean, per-group deviation norms, inverse-norm weights (sirt-mimo-norm.cu:56-118)
+            launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->tmp, c->st);
+            launch_group_dev_norm(c->corr, G, N, c->f, sc, c->tmp, c->part, nb, c->st);
+            launch_sum_parts(c->part, G, nb, c->sums, c->st);
+            std::vector<double> d2(G);
+            CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
+            CU(c, cudaStreamSynchronize(c->st));
+            std::vector<double> w(G);
+            double W = 0.0;
+            for (int gg = 0; gg < G; ++gg) { w[gg] = 1.0 / std::sqrt(d2[gg]); W += w[gg]; }
+            for (int gg = 0; gg < G; ++gg) w[gg] /= W;
+            CU(c, cudaMemcpyAsync(c->sums, w.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
+            launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
+            TRY(apply_dir(c, sch, s));
+            CU(c, cudaStreamSynchronize(c->st));   // w lives on the host stack
+            break;
+        }
+        case TOMO_SIRT_AVG_WEIGHT: {
+            // fg = f + s*mask*df_g; f += sum_g fg/||fg - mean fg|| (sirt-mimo-avg-weight.cu:130-203)
+            launch_avgw_fbar(c->corr, G, N, c->f, c->mask, sc, s, c->tmp, c->st);
+            launch_avgw_norm(c->corr, G, N, c->f, c->mask, sc, s, c->tmp, c->part, nb, c->st);
+            launch_sum_parts(c->part, G, nb, c->sums, c->st);
+            launch_avgw_apply(c->corr, G, N, c->f, c->mask, sc, s, c->sums, c->st);
+            break;
+        }
+        default:
+            return c->fail(TOMO_ERR_ARG, "unknown method %d", method);
+        }
+    }
+    CU(c, cudaEventRecord(c->ev1, c->st));
+    double eps = std::numeric_limits<double>::quiet_NaN();
+    if (have_true) TRY(epsilon(c, &eps));
+    CU(c, cudaStreamSynchronize(c->st));
+    CU(c, cudaGetLastError());
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        stats->epsilon = eps;
+        stats->resid_norm2 = r2;
+        stats->scale = s;
+        stats->seconds = ms * 1e-3;
+        stats->cell_updates = 2.0 * (double)G * (double)(g.nt - 2) * (double)N;
+    }
+    return TOMO_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int32_t tomo_abi_version(void) { return TOMO_ABI_VERSION; }
+
+const char* tomo_status_string(tomo_status s) {
+    switch (s) {
+    case TOMO_OK: return "ok";
+    case TOMO_ERR_ARG: return "invalid argument";
+    case TOMO_ERR_CUDA: return "CUDA error";
+    case TOMO_ERR_OOM: return "out of device memory";
+    case TOMO_ERR_TIMEOUT: return "device wait timed out";
+    case TOMO_ERR_DIVERGED: return "diverged";
+    case TOMO_ERR_IO: return "I/O error";
+    case TOMO_ERR_STATE: return "invalid state";
+    }
+    return "unknown status";
+}
+
+tomo_status tomo_config_init(tomo_config* cfg, int32_t profile) {
+    if (!cfg) return TOMO_ERR_ARG;
+    std::memset(cfg, 0, sizeof *cfg);
+    if (profile == TOMO_PROFILE_REF) {
+        cfg->nx = 192; cfg->ny = 192; cfg->nt = 401;
+        cfg->profile = TOMO_PROFILE_REF;
+        cfg->group_size = 10;
+        cfg->ring_lo = 20; cfg->ring_hi = 180;
+    } else if (profile == TOMO_PROFILE_CFG) {
+        cfg->nx = 128; cfg->ny = 128; cfg->nt = 600;
+        cfg->profile = TOMO_PROFILE_CFG;
+        cfg->group_size = 4;
+        cfg->n_transducers = 32; cfg->radius = 50.f;
+        cfg->courant = 0.5f; cfg->cells_per_wavelength = 12.f;
+        cfg->sponge_width = 16; cfg->sponge_max = 0.05f;
+    } else {
+        return TOMO_ERR_ARG;
+    }
+    return TOMO_OK;
+}
+
+tomo_status tomo_create(const tomo_config* cfg, tomo_ctx** out) {
+    g_create_error.clear();
+    if (!cfg || !out) { g_create_error = "NULL argument"; return TOMO_ERR_ARG; }
+    *out = nullptr;
+    tomo_ctx* c = new (std::nothrow) tomo_ctx();
+    if (!c) return TOMO_ERR_OOM;
+    c->dev = -1;
+    std::string why;
+    tomo_status s = build_geometry(*cfg, c->geo, why);
+    if (s != TOMO_OK) { g_create_error = why; delete c; return s; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        g_create_error = "no CUDA device";
+        delete c;
+        return TOMO_ERR_CUDA;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) { g_create_error = "device ordinal out of range"; delete c; return TOMO_ERR_ARG; }
+    c->dev = cfg->device;
+    if ((s = c->cuda(cudaSetDevice(c->dev), "cudaSetDevice")) == TOMO_OK &&
+        (s = c->cuda(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate")) == TOMO_OK &&
+        (s = c->cuda(cudaEventCreate(&c->ev0), "cudaEventCreate")) == TOMO_OK &&
+        (s = c->cuda(cudaEventCreate(&c->ev1), "cudaEventCreate")) == TOMO_OK && (s = make_plan(c)) == TOMO_OK)
+        s = create_buffers(c);
+    if (s != TOMO_OK) {
+        g_create_error = c->err;
+        delete c;
+        return s;
+    }
+    *out = c;
+    return TOMO_OK;
+}
+
+void tomo_destroy(tomo_ctx* ctx) { delete ctx; }
+
+const char* tomo_last_error(const tomo_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+tomo_status tomo_get_info(const tomo_ctx* c, tomo_info* out) {
+    if (!c || !out) return TOMO_ERR_ARG;
+    out->n_groups = c->geo.G;
+    out->n_channels = c->geo.nch;
+    out->n_transducers = c->geo.ns;
+    out->groups_per_pass = c->P;
+    out->ckpt_interval = c->K;
+    out->n_segments = c->nchunk;
+    out->device_bytes = c->bytes;
+    return TOMO_OK;
+}
+
+void* tomo_stream(const tomo_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+tomo_status tomo_transducers(const tomo_ctx* c, int32_t* ii, int32_t* jj) {
+    if (!c || !ii || !jj) return TOMO_ERR_ARG;
+    std::memcpy(ii, c->geo.ii.data(), sizeof(int32_t) * c->geo.ns);
+    std::memcpy(jj, c->geo.jj.data(), sizeof(int32_t) * c->geo.ns);
+    return TOMO_OK;
+}
+
+tomo_status tomo_phantom_ref(int32_t nx, int32_t ny, float* fo) { return phantom_ref(nx, ny, fo); }
+
+tomo_status tomo_phantom_cfg(int32_t nx, int32_t ny, int32_t kind, int32_t n, float rmin, float rmax, float vmax,
+                             float noise_sigma, float support, uint64_t seed, float* fo) {
+    return phantom_cfg(nx, ny, kind, n, rmin, rmax, vmax, noise_sigma, support, seed, fo);
+}
+
+tomo_status tomo_forward(tomo_ctx* c, const float* f, float* records, float* u_last) {
+    if (!c || !f || !records) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    CU(c, cudaSetDevice(c->dev));
+    const Geometry& g = c->geo;
+    CU(c, cudaMemcpyAsync(c->f, f, sizeof(float) * g.N, cudaMemcpyHostToDevice, c->st));
+    TRY(forward_all(c, u_last));
+    CU(c, cudaMemcpyAsync(records, c->rec, sizeof(float) * (size_t)g.G * c->recs_per_group(),
+                          cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    CU(c, cudaGetLastError());
+    return TOMO_OK;
+}
+
+tomo_status tomo_generate_data(tomo_ctx* c, const float* f_true, float* records, const tomo_noise* noise) {
+    TRY(tomo_forward(c, f_true, records, nullptr));
+    if (noise && noise->kind == 1 && noise->level > 0.f)
+        add_record_noise(records, c->geo.G, c->geo.nt, c->geo.nch, noise->level, noise->seed);
+    else if (noise && noise->kind != 0 && noise->kind != 1)
+        return c->fail(TOMO_ERR_ARG, "unknown noise kind %d", noise->kind);
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_records(tomo_ctx* c, const float* records) {
+    if (!c || !records) return c ? c->fail(TOMO_ERR_ARG, "NULL records") : TOMO_ERR_ARG;
+    CU(c, cudaSetDevice(c->dev));
+    CU(c, cudaMemcpyAsync(c->meas, records, sizeof(float) * (size_t)c->geo.G * c->recs_per_group(),
+                          cudaMemcpyHostToDevice, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    c->meas_set = true;
+    return TOMO_OK;
+}
+
+tomo_status tomo_gradient(tomo_ctx* c, const float* f, const float* records, float* dfg, float* df,
+                          double* resid_norm2) {
+    if (!c || !f) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    if (records) TRY(tomo_set_records(c, records));
+    if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
+    const Geometry& g = c->geo;
+    CU(c, cudaSetDevice(c->dev));
+    CU(c, cudaMemcpyAsync(c->f, f, sizeof(float) * g.N, cudaMemcpyHostToDevice, c->st));
+    TRY(gradient_all(c));
+    if (resid_norm2) TRY(residual_norm(c, resid_norm2));
+    if (dfg) {
+        if (!c->dfg) TRY(c->alloc(&c->dfg, (int64_t)g.G * g.N, "per-group gradients"));
+        for (int gg = 0; gg < g.G; ++gg)
+            launch_combine(c->corr + (int64_t)gg * g.N, 1, g.N, c->f, g.corr_scale, nullptr, 1.0,
+                           c->dfg + (int64_t)gg * g.N, c->st);
+        CU(c, cudaMemcpyAsync(dfg, c->dfg, sizeof(float) * (size_t)g.G * g.N, cudaMemcpyDeviceToHost, c->st));
+    }
+    if (df) {
+        launch_combine(c->corr, g.G, g.N, c->f, g.corr_scale, nullptr, 1.0, c->dir, c->st);
+        CU(c, cudaMemcpyAsync(df, c->dir, sizeof(float) * g.N, cudaMemcpyDeviceToHost, c->st));
+    }
+    CU(c, cudaStreamSynchronize(c->st));
+    CU(c, cudaGetLastError());
+    return TOMO_OK;
+}
+
+tomo_status tomo_iterate(tomo_ctx* c, int32_t method, const tomo_schedule* sched, int32_t iter, float* f_inout,
+                         const float* records, const float* f_true, tomo_iter_stats* stats) {
+    if (!c || !f_inout) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    CU(c, cudaSetDevice(c->dev));
+    if (records) TRY(tomo_set_records(c, records));
+    if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
+    const Geometry& g = c->geo;
+    CU(c, cudaMemcpyAsync(c->f, f_inout, sizeof(float) * g.N, cudaMemcpyHostToDevice, c->st));
+    if (f_true) CU(c, cudaMemcpyAsync(c->ftrue, f_true, sizeof(float) * g.N, cudaMemcpyHostToDevice, c->st));
+    TRY(iterate_core(c, method, sched, iter, f_true != nullptr, stats));
+    CU(c, cudaMemcpyAsync(f_inout, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    return TOMO_OK;
+}
+
+tomo_status tomo_run(tomo_ctx* c, int32_t method, const tomo_schedule* sched, float* f_inout, const float* records,
+                     const float* f_true, float target_epsilon, int32_t max_iters, double* eps_log,
+                     int32_t* iters_done) {
+    if (!c || !f_inout || !f_true) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    CU(c, cudaSetDevice(c->dev));
+    if (records) TRY(tomo_set_records(c, records));
+    if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
+    const Geometry& g = c->geo;
+    CU(c, cudaMemcpyAsync(c->f, f_inout, sizeof(float) * g.N, cudaMemcpyHostToDevice, c->st));
+    CU(c, cudaMemcpyAsync(c->ftrue, f_true, sizeof(float) * g.N, cudaMemcpyHostToDevice, c->st));
+    const int64_t limit = max_iters < 0 ? std::numeric_limits<int32_t>::max() : max_iters;
+    double prev = std::numeric_limits<double>::infinity();
+    tomo_status result = TOMO_OK;
+    int done = 0;
+    for (int64_t it = 0; it < limit; ++it) {
+        tomo_iter_stats st{};
+        TRY(iterate_core(c, method, sched, (int)it, true, &st));
+        if (eps_log && max_iters > 0) eps_log[it] = st.epsilon;
+        done = (int)it + 1;
+        if (st.epsilon <= target_epsilon) break;                         // sirt-mimo.cu:356
+        if (st.epsilon > prev || std::isnan(st.epsilon)) { result = TOMO_ERR_DIVERGED; break; }   // :362
+        prev = st.epsilon;
+    }
+    CU(c, cudaMemcpyAsync(f_inout, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    if (iters_done) *iters_done = done;
+    if (result == TOMO_ERR_DIVERGED) c->err = "epsilon rose or became NaN";
+    return result;
+}
+
+tomo_status tomo_forward_device(tomo_ctx* c, const float* d_f, float* d_records) {
+    if (!c || !d_f || !d_records) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    CU(c, cudaSetDevice(c->dev));
+    const Geometry& g = c->geo;
+    CU(c, cudaMemcpyAsync(c->f, d_f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    TRY(forward_all(c, nullptr));
+    CU(c, cudaMemcpyAsync(d_records, c->rec, sizeof(float) * (size_t)g.G * c->recs_per_group(),
+                          cudaMemcpyDeviceToDevice, c->st));
+    return TOMO_OK;
+}
+
+tomo_status tomo_iterate_device(tomo_ctx* c, int32_t method, const tomo_schedule* sched, int32_t iter, float* d_f,
+                                const float* d_records, const float* d_f_true, tomo_iter_stats* stats) {
+    if (!c || !d_f) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    CU(c, cudaSetDevice(c->dev));
+    const Geometry& g = c->geo;
+    if (d_records) {
+        CU(c, cudaMemcpyAsync(c->meas, d_records, sizeof(float) * (size_t)g.G * c->recs_per_group(),
+                              cudaMemcpyDeviceToDevice, c->st));
+        c->meas_set = true;
+    }
+    if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
+    CU(c, cudaMemcpyAsync(c->f, d_f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    if (d_f_true) CU(c, cudaMemcpyAsync(c->ftrue, d_f_true, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    TRY(iterate_core(c, method, sched, iter, d_f_true != nullptr, stats));
+    CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    return TOMO_OK;
+}
+
+tomo_status tomo_synchronize(tomo_ctx* c) {
+    if (!c) return TOMO_ERR_ARG;
+    CU(c, cudaSetDevice(c->dev));
+    CU(c, cudaStreamSynchronize(c->st));
+    CU(c, cudaGetLastError());
+    return TOMO_OK;
+}
+
+}  // extern "C"

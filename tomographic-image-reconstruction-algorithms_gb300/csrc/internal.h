@@ -1,0 +1,150 @@
+// internal.h -- shared declarations of the engine's host and device code.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "tomo.h"
+
+namespace tomo {
+
+// Reference constants (sirt-mimo.cu:26-35), the float values the reference uses.
+constexpr float kRefH = 0.001f;
+constexpr float kRefDT = 3.3333e-07f;
+constexpr float kRefOmegaC = 7.8540e+05f;
+constexpr float kRefTao = 4.0000e-06f;
+constexpr float kRefTT = 8.1573e-06f;
+
+// Host-side description of one problem: geometry, emitters, receivers.
+struct Geometry {
+    tomo_config cfg{};
+    bool ref = true;
+    int nx = 0, ny = 0, nt = 0;
+    int64_t N = 0;       // nx*ny
+    int G = 0;           // groups
+    int gs = 0;          // group size
+    int ns = 0;          // transducers
+    int nch = 0;         // record channels
+    int lo = 0, hi = 0;  // REF sensor lines
+    std::vector<int32_t> ii, jj;       // transducers (REF 1-based, CFG 0-based cells)
+    std::vector<int32_t> box;          // REF: per group {i0, i1, j0, j1} 0-based inclusive emission box
+    std::vector<int32_t> emit;         // CFG: G*gs emitter cells
+    std::vector<int32_t> rcv;          // receiver cell per channel, -1 none
+    std::vector<int32_t> rid;          // CFG: per-cell channel index or -1
+    std::vector<uint8_t> mask;         // update mask
+    std::vector<float> src;            // per step source factor (REF: h^2 * wavelet(k); CFG: C^2 ricker(n))
+    int n_src_steps = 0;               // steps k (computing u(k+1)) that add a source
+    double corr_scale = 1.0;           // REF 1/h^2, CFG C^2
+};
+
+// Builds the geometry; returns TOMO_OK or TOMO_ERR_ARG with a reason.
+tomo_status build_geometry(const tomo_config& cfg, Geometry& geo, std::string& why);
+tomo_status phantom_ref(int nx, int ny, float* fo);
+tomo_status phantom_cfg(int nx, int ny, int kind, int n, float rmin, float rmax, float vmax,
+                        float noise_sigma, float support, uint64_t seed, float* fo);
+// rec += level * std(trace) * N(0,1) per (group, channel) trace, seeded.
+void add_record_noise(float* rec, int G, int nt, int nch, float level, uint64_t seed);
+
+// splitmix64-based portable RNG (identical on x86 and Arm).
+struct Rng {
+    uint64_t s;
+    explicit Rng(uint64_t seed) : s(seed ^ 0x9E3779B97F4A7C15ull) {}
+    uint64_t next() {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+    double normal();
+};
+
+// ---- device-side argument blocks -------------------------------------------------
+struct DevGeo {
+    int nx, ny, nt, nch;
+    int lo, hi;            // REF sensor lines
+    int gs;                // CFG emitters per group
+    int sponge_w;          // CFG
+    float sponge_max;      // CFG
+    const int32_t* box;    // REF per-group emission box (4 ints), global group index
+    const int32_t* emit;   // CFG emitter cells, global group index
+    const int32_t* rcv;    // receiver cell per channel
+    const int32_t* rid;    // CFG per-cell channel or -1
+    const float* src;      // per step source factor
+    int n_src_steps;
+};
+
+struct FwdStep {
+    const float* up;   // slice k-1 of pass-group 0
+    const float* uc;   // slice k
+    float* un;         // slice k+1
+    int64_t gstride;   // elements between consecutive groups of the pass
+    float* ck;         // optional checkpoint copy of slice k+1 (pass-group 0), or null
+    int64_t ckstride;
+    int k;             // computing slice k+1
+    int g0;            // global index of pass-group 0
+    int ng;            // groups in the pass
+};
+
+struct AdjStep {
+    const float* z2;   // z(k+2)
+    const float* z1;   // z(k+1)
+    float* zk;         // z(k) output
+    int64_t zstride;
+    const float* uq;   // forward slice correlated with z(k): REF u(k), CFG u(k-1)
+    int64_t ustride;
+    const float* rr;   // residual records of pass-group 0 at step k: rr + k*nch
+    int64_t rrstride;  // elements between groups in rr (nt*nch)
+    float* corr;       // per-group correlation accumulators of pass-group 0
+    int64_t cstride;
+    int k;
+    int ng;
+};
+
+struct GatherStep {
+    const float* u;      // slice k of pass-group 0
+    int64_t gstride;
+    const float* meas;   // measured records of pass-group 0 (g*nt*nch layout) or null
+    float* out;          // pass-group 0 records (simulated if meas null, residual otherwise)
+    double* part;        // per (group, k) squared residual, pass-group 0, stride nt; or null
+    int k;
+    int ng;
+};
+
+// ---- kernel launchers (kernels.cu) --------------------------------------------------
+void launch_coef(int profile, const float* f, float* coef, float* rcoef, int64_t N, float courant,
+                 void* stream);
+void launch_fwd_step(int profile, const DevGeo& g, const float* coef, const float* rcoef,
+                     const FwdStep& s, void* stream);
+void launch_adj_step(int profile, const DevGeo& g, const float* coef, const AdjStep& s, void* stream);
+void launch_gather(const DevGeo& g, const GatherStep& s, void* stream);
+void launch_fill(float* p, int64_t n, float v, void* stream);
+// zero slots off0 and off1 (element offsets) of ng groups spaced gstride apart
+void launch_zero_slots(float* base, int ng, int64_t gstride, int64_t off0, int64_t off1, int64_t N, void* stream);
+// copy ng groups: dst[gl*dstride + q] = src[gl*sstride + q], q < N
+void launch_copy_groups(float* dst, int64_t dstride, const float* src, int64_t sstride, int ng, int64_t N, void* stream);
+
+// reductions and update rules (deterministic, FP64 where stated)
+// dfg(g) = corr(g) * scale / (1 + f); dir = sum_g w_g dfg(g) (w may be null: all 1) times post
+void launch_combine(const float* corr, int G, int64_t N, const float* f, double scale,
+                    const double* w, double post, float* dir, void* stream);
+// part[g*nb + b] = block partial of sum_q (corr(g)*scale/(1+f) - mean)^2, mean = dir/G-ish supplied
+void launch_group_dev_norm(const float* corr, int G, int64_t N, const float* f, double scale,
+                           const float* mean, double* part, int nb, void* stream);
+// avg-weight: part[g*nb+b] partial of sum_q (f + s*mask*dfg - fbar)^2
+void launch_avgw_norm(const float* corr, int G, int64_t N, const float* f, const uint8_t* mask,
+                      double scale, double s, const float* fbar, double* part, int nb, void* stream);
+void launch_avgw_fbar(const float* corr, int G, int64_t N, const float* f, const uint8_t* mask,
+                      double scale, double s, float* fbar, void* stream);
+void launch_avgw_apply(const float* corr, int G, int64_t N, float* f, const uint8_t* mask,
+                       double scale, double s, const double* w, void* stream);
+void launch_sum_parts(const double* part, int rows, int nb, double* out, void* stream);
+void launch_maxabs(const float* dir, const uint8_t* mask, int64_t N, unsigned int* out, void* stream);
+void launch_apply(float* f, const float* dir, const uint8_t* mask, int64_t N, double s,
+                  const unsigned int* maxabs, void* stream);
+void launch_eps_parts(const float* f, const float* fo, int64_t N, double* part, int nb, void* stream);
+
+int reduce_blocks();  // number of partial blocks the reductions use
+
+}  // namespace tomo

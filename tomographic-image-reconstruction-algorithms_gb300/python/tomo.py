@@ -1,0 +1,303 @@
+"""Python binding of libtomo.so, the C ABI declared in include/tomo.h.
+
+This module is a thin ctypes layer used by the tests, the benchmark and
+notebook users.  All compute runs in libtomo.so's CUDA kernels; nothing here
+computes a wavefield.  Importing the module does not load the library; the
+first call to :func:`lib` does, and raises if the CUDA library is missing
+(there is no CPU fallback).
+
+Array conventions follow include/tomo.h: FP32, i (x) fastest, records laid out
+as ``rec[g, k, c]`` (groups, time steps, channels).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REPO_DIR = os.path.dirname(PKG_DIR)
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libtomo.so")
+
+# tomo_status
+OK, ERR_ARG, ERR_CUDA, ERR_OOM, ERR_TIMEOUT, ERR_DIVERGED, ERR_IO, ERR_STATE = range(8)
+# tomo_profile
+PROFILE_REF, PROFILE_CFG = 0, 1
+# tomo_method
+SIRT_CLASSIC, SIRT_SCALED, SIRT_NORM, SIRT_WEIGHT, SIRT_AVG, SIRT_AVG_WEIGHT, ART = range(7)
+METHOD_NAMES = {
+    SIRT_CLASSIC: "sirt-classic", SIRT_SCALED: "sirt-scaled", SIRT_NORM: "sirt-norm",
+    SIRT_WEIGHT: "sirt-weight", SIRT_AVG: "sirt-avg", SIRT_AVG_WEIGHT: "sirt-avg-weight",
+    ART: "art",
+}
+# tomo_sched_kind
+SCHED_CONST, SCHED_POWER, SCHED_LINEAR = range(3)
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nt", C.c_int32),
+        ("profile", C.c_int32), ("group_size", C.c_int32),
+        ("ring_lo", C.c_int32), ("ring_hi", C.c_int32),
+        ("n_transducers", C.c_int32), ("radius", C.c_float), ("courant", C.c_float),
+        ("cells_per_wavelength", C.c_float), ("sponge_width", C.c_int32),
+        ("sponge_max", C.c_float),
+        ("ckpt_interval", C.c_int32), ("groups_per_pass", C.c_int32), ("device", C.c_int32),
+        ("reserved", C.c_int32 * 4),
+    ]
+
+
+class Schedule(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32), ("omega", C.c_float), ("alpha", C.c_float),
+        ("beta", C.c_float), ("gamma", C.c_float), ("normalize", C.c_int32),
+        ("reserved", C.c_int32 * 2),
+    ]
+
+
+class IterStats(C.Structure):
+    _fields_ = [
+        ("epsilon", C.c_double), ("resid_norm2", C.c_double), ("scale", C.c_double),
+        ("seconds", C.c_double), ("cell_updates", C.c_double),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("n_groups", C.c_int32), ("n_channels", C.c_int32), ("n_transducers", C.c_int32),
+        ("groups_per_pass", C.c_int32), ("ckpt_interval", C.c_int32),
+        ("n_segments", C.c_int32), ("device_bytes", C.c_int64),
+    ]
+
+
+class Noise(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("level", C.c_float), ("seed", C.c_uint64)]
+
+
+def ref_config(nx=192, ny=192, nt=401, group_size=10, ring_lo=20, ring_hi=180, **kw) -> Config:
+    """The reference problem (sirt-mimo.cu:17-35), optionally resized."""
+    c = Config(nx=nx, ny=ny, nt=nt, profile=PROFILE_REF, group_size=group_size,
+               ring_lo=ring_lo, ring_hi=ring_hi)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def cfg_config(nx=128, ny=128, nt=600, n_transducers=32, group_size=4, radius=50.0,
+               courant=0.5, cells_per_wavelength=12.0, sponge_width=16, sponge_max=0.05,
+               **kw) -> Config:
+    """A synthetic-workload problem (defaults: the 128^2 / 32-transducer case)."""
+    c = Config(nx=nx, ny=ny, nt=nt, profile=PROFILE_CFG, group_size=group_size,
+               n_transducers=n_transducers, radius=radius, courant=courant,
+               cells_per_wavelength=cells_per_wavelength, sponge_width=sponge_width,
+               sponge_max=sponge_max)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def schedule(kind=SCHED_CONST, omega=1.0, alpha=0.0, beta=0.0, gamma=1.0, normalize=0) -> Schedule:
+    return Schedule(kind=kind, omega=omega, alpha=alpha, beta=beta, gamma=gamma, normalize=normalize)
+
+
+def n_groups(cfg: Config) -> int:
+    ns = 4 * (cfg.ring_hi - cfg.ring_lo) if cfg.profile == PROFILE_REF else cfg.n_transducers
+    return ns // cfg.group_size
+
+
+def n_channels(cfg: Config) -> int:
+    return 4 * cfg.nx if cfg.profile == PROFILE_REF else cfg.n_transducers
+
+
+_LIB = None
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def lib(path: str | None = None) -> C.CDLL:
+    """Load libtomo.so (built in-tree by the package build)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libtomo.so not built at {p}; run __graft_entry__.build()")
+    L = C.CDLL(p)
+    vp, i32, f32, u64 = C.c_void_p, C.c_int32, C.c_float, C.c_uint64
+    FP, DP, IP = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    sig = {
+        "tomo_abi_version": (i32, []),
+        "tomo_status_string": (C.c_char_p, [i32]),
+        "tomo_config_init": (i32, [C.POINTER(Config), i32]),
+        "tomo_create": (i32, [C.POINTER(Config), C.POINTER(vp)]),
+        "tomo_destroy": (None, [vp]),
+        "tomo_last_error": (C.c_char_p, [vp]),
+        "tomo_get_info": (i32, [vp, C.POINTER(Info)]),
+        "tomo_stream": (vp, [vp]),
+        "tomo_transducers": (i32, [vp, IP, IP]),
+        "tomo_phantom_ref": (i32, [i32, i32, FP]),
+        "tomo_phantom_cfg": (i32, [i32, i32, i32, i32, f32, f32, f32, f32, f32, u64, FP]),
+        "tomo_forward": (i32, [vp, FP, FP, FP]),
+        "tomo_generate_data": (i32, [vp, FP, FP, C.POINTER(Noise)]),
+        "tomo_set_records": (i32, [vp, FP]),
+        "tomo_gradient": (i32, [vp, FP, FP, FP, FP, DP]),
+        "tomo_iterate": (i32, [vp, i32, C.POINTER(Schedule), i32, FP, FP, FP, C.POINTER(IterStats)]),
+        "tomo_run": (i32, [vp, i32, C.POINTER(Schedule), FP, FP, FP, f32, i32, DP, IP]),
+        "tomo_forward_device": (i32, [vp, vp, vp]),
+        "tomo_iterate_device": (i32, [vp, i32, C.POINTER(Schedule), i32, vp, vp, vp, C.POINTER(IterStats)]),
+        "tomo_synchronize": (i32, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+class TomoError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"tomo status {status}: {msg}")
+        self.status = status
+
+
+def phantom_ref(nx=192, ny=192) -> np.ndarray:
+    fo = np.zeros((ny, nx), np.float32)
+    st = lib().tomo_phantom_ref(nx, ny, _fp(fo))
+    if st:
+        raise TomoError(st, "tomo_phantom_ref")
+    return fo
+
+
+def phantom_cfg(nx, ny, kind, n, rmin, rmax, vmax, noise_sigma, support, seed) -> np.ndarray:
+    fo = np.zeros((ny, nx), np.float32)
+    st = lib().tomo_phantom_cfg(nx, ny, kind, n, rmin, rmax, vmax, noise_sigma, support, seed, _fp(fo))
+    if st:
+        raise TomoError(st, "tomo_phantom_cfg")
+    return fo
+
+
+class Context:
+    """Owns a tomo_ctx (device buffers and one CUDA stream)."""
+
+    def __init__(self, cfg: Config):
+        self.cfg = cfg
+        h = C.c_void_p()
+        st = lib().tomo_create(C.byref(cfg), C.byref(h))
+        if st:
+            raise TomoError(st, "tomo_create: " + (lib().tomo_last_error(None) or b"").decode())
+        self.h = h
+        info = Info()
+        self._check(lib().tomo_get_info(self.h, C.byref(info)))
+        self.info = info
+        self.G = info.n_groups
+        self.nch = info.n_channels
+
+    def _check(self, st):
+        if st:
+            raise TomoError(st, (lib().tomo_last_error(self.h) or b"").decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().tomo_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def shape(self):
+        return (self.cfg.ny, self.cfg.nx)
+
+    def records_shape(self):
+        return (self.G, self.cfg.nt, self.nch)
+
+    def transducers(self):
+        n = self.info.n_transducers
+        ii = np.zeros(n, np.int32)
+        jj = np.zeros(n, np.int32)
+        self._check(lib().tomo_transducers(self.h, _ip(ii), _ip(jj)))
+        return ii, jj
+
+    def forward(self, f, u_last=False):
+        f = np.ascontiguousarray(f, np.float32)
+        rec = np.zeros(self.records_shape(), np.float32)
+        ul = np.zeros((self.G,) + self.shape, np.float32) if u_last else None
+        self._check(lib().tomo_forward(self.h, _fp(f), _fp(rec), _fp(ul)))
+        return (rec, ul) if u_last else rec
+
+    def generate_data(self, f_true, noise_level=0.0, seed=0):
+        f = np.ascontiguousarray(f_true, np.float32)
+        rec = np.zeros(self.records_shape(), np.float32)
+        nz = Noise(kind=1 if noise_level > 0 else 0, level=noise_level, seed=seed)
+        self._check(lib().tomo_generate_data(self.h, _fp(f), _fp(rec), C.byref(nz)))
+        return rec
+
+    def set_records(self, rec):
+        rec = np.ascontiguousarray(rec, np.float32)
+        self._check(lib().tomo_set_records(self.h, _fp(rec)))
+
+    def gradient(self, f, rec, per_group=True):
+        f = np.ascontiguousarray(f, np.float32)
+        rec = np.ascontiguousarray(rec, np.float32)
+        dfg = np.zeros((self.G,) + self.shape, np.float32) if per_group else None
+        df = np.zeros(self.shape, np.float32)
+        r2 = C.c_double()
+        self._check(lib().tomo_gradient(self.h, _fp(f), _fp(rec), _fp(dfg), _fp(df), C.byref(r2)))
+        return dfg, df, r2.value
+
+    def iterate(self, method, sched: Schedule, it, f, rec=None, f_true=None):
+        """One iteration in place on f (float32 array); returns IterStats."""
+        assert f.dtype == np.float32 and f.flags.c_contiguous
+        rp = None if rec is None else _fp(np.ascontiguousarray(rec, np.float32))
+        ft = None if f_true is None else np.ascontiguousarray(f_true, np.float32)
+        stats = IterStats()
+        self._check(lib().tomo_iterate(self.h, method, C.byref(sched), it, _fp(f), rp, _fp(ft),
+                                       C.byref(stats)))
+        return stats
+
+    def run(self, method, sched, f, rec, f_true, target_eps, max_iters):
+        assert f.dtype == np.float32 and f.flags.c_contiguous
+        log = np.zeros(max(max_iters, 1), np.float64)
+        done = C.c_int32()
+        st = lib().tomo_run(self.h, method, C.byref(sched), _fp(f),
+                            _fp(np.ascontiguousarray(rec, np.float32)),
+                            _fp(np.ascontiguousarray(f_true, np.float32)),
+                            target_eps, max_iters, _dp(log), C.byref(done))
+        if st not in (OK, ERR_DIVERGED):
+            self._check(st)
+        return log[: done.value], st
+
+    def forward_device(self, d_f: int, d_rec: int):
+        self._check(lib().tomo_forward_device(self.h, C.c_void_p(d_f), C.c_void_p(d_rec)))
+
+    def iterate_device(self, method, sched, it, d_f: int, d_rec: int = 0, d_ftrue: int = 0):
+        stats = IterStats()
+        self._check(lib().tomo_iterate_device(self.h, method, C.byref(sched), it, C.c_void_p(d_f),
+                                              C.c_void_p(d_rec or None), C.c_void_p(d_ftrue or None),
+                                              C.byref(stats)))
+        return stats
+
+    def synchronize(self):
+        self._check(lib().tomo_synchronize(self.h))
+
+    @property
+    def stream(self) -> int:
+        return lib().tomo_stream(self.h) or 0
