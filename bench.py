@@ -1,0 +1,364 @@
+#!/usr/bin/env python3
+"""Benchmark of the reconstruction hot path: one plain weighted SIRT iteration.
+
+Workload (default): 512x512 grid, nt 2500, Courant 0.5, 16-cell quadratic
+sponge, 256 transducers on a radius-220 circle in 32 groups of 8, Ricker
+source at 12 cells per wavelength, forward history checkpointed every 50
+steps; phantom of 8 seeded ellipses plus smoothed noise, records with 1%
+Gaussian noise (synthetic, seeded).  A step is one normalised-weight SIRT
+iteration: forward sweep of all 32 groups, residual, adjoint sweep with the
+fused correlation, checkpoint recompute, and the update.
+
+metric: stencil GB/s, algorithmic bytes per iteration = G*nx*ny*(nt-2)*(16+20)
+(16 B per forward and 20 B per adjoint cell-update; recompute not credited).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl tomo|reference]
+                    [--workload c2|c1|ref192|c5]
+Under torchrun each rank reconstructs its own independent phantom on its own
+GPU (weak scaling over independent reconstructions, no collective on the
+data path); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "tomographic-image-reconstruction-algorithms_gb300")
+sys.path.insert(0, os.path.join(PKG, "python"))
+sys.path.insert(0, PKG)
+
+import numpy as np  # noqa: E402
+
+import tomo  # noqa: E402
+
+WORKLOADS = {
+    "c2": dict(desc="512x512, nt 2500, 256 transducers r=220, 32 groups of 8, sponge 16/0.05, "
+                    "Ricker 12 cells/wavelength, checkpoint every 50 steps, plain weighted SIRT",
+               cfg=dict(nx=512, ny=512, nt=2500, n_transducers=256, group_size=8, radius=220.0,
+                        ckpt_interval=50),
+               phantom=(1, 8, 10.0, 60.0, 0.15, 0.01, 176.0), noise=0.01,
+               method=tomo.SIRT_NORM, sched=dict(omega=0.02, normalize=1)),
+    "c1": dict(desc="128x128, nt 600, 32 transducers r=50, 8 groups of 4, plain uniform SIRT step 0.1",
+               cfg=dict(nx=128, ny=128, nt=600, n_transducers=32, group_size=4, radius=50.0),
+               phantom=(0, 3, 5.0, 15.0, 0.1, 0.0, 40.0), noise=0.0,
+               method=tomo.SIRT_CLASSIC, sched=dict(omega=0.1, normalize=1)),
+    "c5": dict(desc="2048x2048, nt 8000, 512 transducers r=950, 64 groups of 8, checkpoint every 200 steps",
+               cfg=dict(nx=2048, ny=2048, nt=8000, n_transducers=512, group_size=8, radius=950.0,
+                        ckpt_interval=200),
+               phantom=(1, 16, 20.0, 240.0, 0.15, 0.01, 760.0), noise=0.01,
+               method=tomo.SIRT_NORM, sched=dict(omega=0.02, normalize=1)),
+    "ref192": dict(desc="reference problem: 192x192, nt 401, 640 transducers on the square ring, "
+                        "group size 10 (64 groups), normalised SIRT",
+                   cfg=None, phantom=None, noise=0.0, method=tomo.SIRT_NORM,
+                   sched=dict(kind=tomo.SCHED_POWER, omega=1e5, alpha=0.5, beta=0.5, gamma=1.0)),
+}
+
+
+def make_config(w, device):
+    if w["cfg"] is None:
+        return tomo.ref_config(device=device)
+    return tomo.cfg_config(device=device, **w["cfg"])
+
+
+def make_phantom(w, cfg, seed):
+    if w["phantom"] is None:
+        return tomo.phantom_ref()
+    kind, n, rmin, rmax, vmax, sig, sup = w["phantom"]
+    return tomo.phantom_cfg(cfg.nx, cfg.ny, kind, n, rmin, rmax, vmax, sig, sup, seed)
+
+
+def algorithmic_bytes(cfg, G):
+    return float(G) * cfg.nx * cfg.ny * (cfg.nt - 2) * 36.0
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        self.tmp.flush()
+        try:
+            rows = [r.split(",") for r in open(self.tmp.name).read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample(w, cfg, fo, rec, target_s=12.0):
+    """Oracle FP32 OpenMP forward+adjoint sweeps of whole groups (all host threads)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_lib as O
+
+    O.build()
+    cores = os.cpu_count() or 1
+    f64 = np.zeros(fo.shape, np.float64)
+    t0 = time.perf_counter()
+    cu = 0.0
+    ng = 0
+    while True:
+        cu += O.sweep(cfg, f64, rec, ng % tomo.n_groups(cfg), 1, prec=32, threads=cores)
+        ng += 1
+        if time.perf_counter() - t0 > target_s or ng >= tomo.n_groups(cfg):
+            break
+    dt = time.perf_counter() - t0
+    gbs = cu / 2 * 36.0 / dt / 1e9
+    return {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": f"{ng} group forward+adjoint sweep(s) of the full {cfg.nx}x{cfg.ny}x{cfg.nt} problem, "
+                      f"oracle FP32 transcription, OpenMP over {cores} threads, {dt:.1f} s",
+            "seconds": dt, "cell_updates": cu}
+
+
+def reference_arm(args, w, rank, world):
+    if rank != 0:
+        return
+    cfg = make_config(w, 0)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_lib as O
+
+    O.build()
+    G = tomo.n_groups(cfg)
+    nch = tomo.n_channels(cfg)
+    # the sweep's work does not depend on the values: homogeneous field, zero data
+    rec = np.zeros((G, cfg.nt, nch), np.float32)
+    cores = os.cpu_count() or 1
+    f64 = np.zeros((cfg.ny, cfg.nx), np.float64)
+    for _ in range(args.warmup):
+        O.sweep(cfg, f64, rec, 0, 1, prec=32, threads=cores)
+    ts = []
+    cu = 0.0
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        cu = O.sweep(cfg, f64, rec, s % G, 1, prec=32, threads=cores)
+        ts.append(time.perf_counter() - t0)
+    dt = sum(ts)
+    gbs = cu * args.steps / 2 * 36.0 / dt / 1e9
+    line = {
+        "impl": "reference", "metric": metric_name(), "value": gbs, "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded phantom)", "config": {"workload": args.workload + ": " + w["desc"]},
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port",
+                         "sample": "each step: one group's forward+adjoint sweep of the full problem, oracle FP32 "
+                                   "transcription of the reference kernels (the reference ships no CPU path)"},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def metric_name():
+    return "stencil GB/s (algorithmic 36 B per forward+adjoint cell-update) of one plain weighted SIRT iteration"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="tomo", choices=["tomo", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        import torch
+
+        dist = dist_mod
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+
+    if args.impl == "reference":
+        reference_arm(args, w, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    import torch
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (libtomo.so has no CPU path)")
+    tomo.lib()
+    cfg = make_config(w, local)
+    fo = make_phantom(w, cfg, 2001 + 1000 * rank)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        # the oracle runs before the first GPU call of this process
+        G0 = tomo.n_groups(cfg)
+        cpu = cpu_sample(w, cfg, fo, np.zeros((G0, cfg.nt, tomo.n_channels(cfg)), np.float32))
+
+    ctx = tomo.Context(cfg)
+    G = ctx.G
+    rec = ctx.generate_data(fo, noise_level=w["noise"], seed=77 + rank)
+    sched = tomo.schedule(**w["sched"])
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    d_f = torch.zeros(fo.shape, dtype=torch.float32, device=dev)
+    d_ft = torch.from_numpy(fo).to(dev)
+    d_rec = torch.from_numpy(rec).to(dev)
+    torch.cuda.synchronize(dev)
+    # records go to the context once; each step then reads them from HBM
+    ctx.iterate_device(w["method"], sched, 0, d_f.data_ptr(), d_rec.data_ptr(), d_ft.data_ptr())
+    ctx.synchronize()
+    for it in range(1, args.warmup):
+        ctx.iterate_device(w["method"], sched, it, d_f.data_ptr(), 0, d_ft.data_ptr())
+    ctx.synchronize()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    launches = 0.0
+    eps = []
+    barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for s in range(args.steps):
+            st = ctx.iterate_device(w["method"], sched, args.warmup + s, d_f.data_ptr(), 0, d_ft.data_ptr())
+            launches += st.kernel_launches
+            eps.append(st.epsilon)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.summary()
+    t_max = ms
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev if dist.get_backend() == "nccl" else "cpu")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    bytes_step = algorithmic_bytes(cfg, G)
+    value = world * bytes_step * args.steps / (t_max * 1e-3) / 1e9
+
+    # end to end through the public host-buffer API: pinned f and records in, f out, every step
+    f_host = torch.zeros(fo.shape, dtype=torch.float32).pin_memory()
+    rec_host = torch.from_numpy(rec).pin_memory()
+    ft_host = torch.from_numpy(fo).pin_memory()
+    fa = f_host.numpy()
+    barrier()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        ctx.iterate(w["method"], sched, s, fa, rec_host.numpy(), ft_host.numpy())
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    e2e_max = e2e_s
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev if dist.get_backend() == "nccl" else "cpu")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_max = float(t.item())
+    e2e_val = world * bytes_step * args.steps / e2e_max / 1e9
+    h2d = 4 * (fo.size * 2 + rec.size)
+    d2h = 4 * fo.size + 8
+
+    # roofline of the dominant kernel, timed live on the context stream
+    info = ctx.info
+    nt, K, nseg = cfg.nt, info.ckpt_interval, info.n_segments
+    fwd_launches = (nt - 2) + (0 if nseg == 1 else (nseg - 1) * (K - 1))
+    adj_launches = nt - 2
+    fwd_ms, fwd_b = ctx.time_kernel(0, 200)
+    adj_ms, adj_b = ctx.time_kernel(1, 200)
+    share_f = fwd_launches * fwd_ms
+    share_a = adj_launches * adj_ms
+    dom = ("forward_step", fwd_ms, fwd_b) if share_f >= share_a else ("adjoint_step", adj_ms, adj_b)
+    peak, peak_kind = peaks()
+    achieved = dom[2] / (dom[1] * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom[0])
+        except Exception:
+            traffic = None
+
+    if rank == 0:
+        line = {
+            "metric": metric_name(), "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded ellipse phantom + smoothed noise, 1% Gaussian record noise)",
+            "config": {"workload": args.workload + ": " + w["desc"], "groups": G,
+                       "groups_per_pass": info.groups_per_pass, "ckpt_interval": K,
+                       "l2": "inputs larger than L2 (%.1f GB resident working set)" % (info.device_bytes / 1e9),
+                       "parallelism": f"replicas{world}" if world > 1 else "single GPU"},
+            "sirt_iter_per_s": world * args.steps / (t_max * 1e-3),
+            "cell_updates_per_s": world * 2.0 * G * cfg.nx * cfg.ny * (nt - 2) * args.steps / (t_max * 1e-3),
+            "epsilon_last": eps[-1] if eps else None,
+            "gpu_launches": launches,
+            "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"kernel": dom[0], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "ms_per_launch": dom[1], "bytes_per_launch": dom[2],
+                         "other": {"forward_step_GBps": fwd_b / (fwd_ms * 1e-3) / 1e9,
+                                   "adjoint_step_GBps": adj_b / (adj_ms * 1e-3) / 1e9}},
+            "clocks": clocks,
+        }
+        if cpu:
+            line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

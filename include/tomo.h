@@ -114,6 +114,7 @@ typedef struct tomo_iter_stats {
     double scale;          /* step size used */
     double seconds;        /* device time of the iteration */
     double cell_updates;   /* forward + adjoint cell-updates credited (no recompute) */
+    double kernel_launches;/* kernels launched by the iteration (graph nodes included) */
 } tomo_iter_stats;
 
 typedef struct tomo_info {
@@ -205,6 +206,15 @@ tomo_status tomo_iterate_device(tomo_ctx* ctx, int32_t method, const tomo_schedu
                                 int32_t iter, float* d_f, const float* d_records,
                                 const float* d_f_true, tomo_iter_stats* stats);
 tomo_status tomo_synchronize(tomo_ctx* ctx);
+
+/* Profiling hook (no reference counterpart): runs `steps` consecutive time steps
+ * of one hot kernel for the first pass's groups on the context stream, bracketed
+ * by CUDA events, after at least one tomo_iterate.  which: 0 forward step,
+ * 1 adjoint step.  Returns the mean duration of one launch and the algorithmic
+ * bytes one launch moves (16 B forward / 20 B adjoint per cell-update).
+ * Clobbers the iteration's scratch state (the next tomo_iterate rebuilds it). */
+tomo_status tomo_time_kernel(tomo_ctx* ctx, int32_t which, int32_t steps,
+                             double* ms_per_launch, double* bytes_per_launch);
 
 #ifdef __cplusplus
 }

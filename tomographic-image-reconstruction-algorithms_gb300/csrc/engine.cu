@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -61,6 +62,11 @@ struct tomo_ctx {
     int64_t bytes = 0;
     bool meas_set = false;
     std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+    std::map<std::tuple<int, int, int>, int64_t> graph_kernels;   // kernel nodes per graph
+    int64_t launches = 0;                                          // kernels issued since reset
+    bool strip = false;          // warp-strip kernels (CFG, nx % 4 == 0)
+    int rows_fwd = 8, rows_adj = 8;
+    bool tuned = false;
     std::vector<void*> allocs;
 
     tomo_status fail(tomo_status s, const char* fmt, ...) {
@@ -118,6 +124,82 @@ struct tomo_ctx {
 namespace {
 
 enum Mode { MODE_FWD = 0, MODE_GRAD = 1 };
+
+void fwd_launch(tomo_ctx* c, const FwdStep& fs) {
+    if (c->strip) launch_fwd_strip(c->rows_fwd, c->dg, c->coef, fs, c->st);
+    else launch_fwd_step(c->geo.cfg.profile, c->dg, c->coef, c->rcoef, fs, c->st);
+}
+
+void adj_launch(tomo_ctx* c, const AdjStep& as) {
+    if (c->strip) launch_adj_strip(c->rows_adj, c->dg, c->coef, as, c->st);
+    else launch_adj_step(c->geo.cfg.profile, c->dg, c->coef, as, c->st);
+}
+
+FwdStep fwd_args(tomo_ctx* c, int k, int g0, int ng) {
+    FwdStep fs{};
+    fs.up = c->hist + c->slot(k - 1);
+    fs.uc = c->hist + c->slot(k);
+    fs.un = c->hist + c->slot(k + 1);
+    fs.gstride = (int64_t)c->S * c->geo.N;
+    fs.k = k;
+    fs.g0 = g0;
+    fs.ng = ng;
+    return fs;
+}
+
+AdjStep adj_args(tomo_ctx* c, int q, int g0, int ng) {
+    const int64_t N = c->geo.N;
+    const int kz = (c->geo.cfg.profile == TOMO_PROFILE_REF) ? q : q + 1;
+    AdjStep as{};
+    as.z2 = c->z + (int64_t)((kz + 2) % 3) * N;
+    as.z1 = c->z + (int64_t)((kz + 1) % 3) * N;
+    as.zk = c->z + (int64_t)(kz % 3) * N;
+    as.zstride = 3 * N;
+    as.uq = c->hist + c->slot(q);
+    as.ustride = (int64_t)c->S * N;
+    as.rr = c->rr + (int64_t)kz * c->geo.nch;
+    as.rrstride = c->recs_per_group();
+    as.corr = c->corr + (int64_t)g0 * N;
+    as.cstride = N;
+    as.k = kz;
+    as.ng = ng;
+    return as;
+}
+
+// Picks rows per warp of the strip kernels by timing each candidate on this
+// problem (a few mid-sweep steps of the first pass); TOMO_STRIP_ROWS=<n> fixes it.
+tomo_status autotune(tomo_ctx* c) {
+    if (c->tuned || !c->strip) { c->tuned = true; return TOMO_OK; }
+    c->tuned = true;
+    if (const char* e = std::getenv("TOMO_STRIP_ROWS")) {
+        c->rows_fwd = c->rows_adj = std::atoi(e);
+        return TOMO_OK;
+    }
+    const int cands[5] = {2, 4, 8, 16, 32};
+    const int nt = c->geo.nt, ng = c->P, reps = 6;
+    const int k0 = std::max(1, nt / 2 - reps);
+    float best_f = 1e30f, best_a = 1e30f;
+    for (int rows : cands) {
+        if (rows > 4 * c->geo.ny) continue;
+        for (int which = 0; which < 2; ++which) {
+            float ms = 0.f;
+            for (int pass = 0; pass < 2; ++pass) {   // first pass warms up
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                for (int t = 0; t < reps; ++t) {
+                    if (which == 0) launch_fwd_strip(rows, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), c->st);
+                    else launch_adj_strip(rows, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, ng), c->st);
+                }
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            }
+            if (which == 0 && ms < best_f) { best_f = ms; c->rows_fwd = rows; }
+            if (which == 1 && ms < best_a) { best_a = ms; c->rows_adj = rows; }
+        }
+    }
+    CU(c, cudaGetLastError());
+    return TOMO_OK;
+}
 
 // Chosen memory plan.
 tomo_status make_plan(tomo_ctx* c) {
@@ -210,11 +292,18 @@ tomo_status create_buffers(tomo_ctx* c) {
     d.sponge_w = g.cfg.sponge_width; d.sponge_max = g.cfg.sponge_max;
     d.box = c->box; d.emit = c->emit; d.rcv = c->rcv; d.rid = c->rid; d.src = c->src;
     d.n_src_steps = g.n_src_steps;
+    c->strip = strip_supported(d, g.cfg.profile) && !std::getenv("TOMO_NO_STRIP");
+    CU(c, cudaMemsetAsync(c->hist, 0, sizeof(float) * (size_t)P * c->S * N, c->st));
+    CU(c, cudaMemsetAsync(c->z, 0, sizeof(float) * (size_t)P * 3 * N, c->st));
+    CU(c, cudaMemsetAsync(c->corr, 0, sizeof(float) * (size_t)G * N, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
     return TOMO_OK;
 }
 
 // Records the launch sequence of one pass (groups g0 .. g0+ng-1) on the stream.
-void record_pass(tomo_ctx* c, int mode, int g0, int ng) {
+// Kernel nodes the recorded pass contains (each launch_* call below is one kernel).
+int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
+    int64_t n = 0;
     const Geometry& g = c->geo;
     const int nt = g.nt, S = c->S, K = c->K;
     const int64_t N = g.N, gstride = (int64_t)S * N, nch = g.nch, rpg = c->recs_per_group();
@@ -222,15 +311,11 @@ void record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     const int prof = g.cfg.profile;
     // ---- forward sweep
     launch_zero_slots(c->hist, ng, gstride, c->slot(0), c->slot(1), N, st);
+    ++n;
+    const float* meas_g = c->meas + (int64_t)g0 * rpg;
+    float* out_g = mode == MODE_GRAD ? c->rr : c->rec + (int64_t)g0 * rpg;
     for (int k = 1; k <= nt - 2; ++k) {
-        FwdStep fs{};
-        fs.up = c->hist + c->slot(k - 1);
-        fs.uc = c->hist + c->slot(k);
-        fs.un = c->hist + c->slot(k + 1);
-        fs.gstride = gstride;
-        fs.k = k;
-        fs.g0 = g0;
-        fs.ng = ng;
+        FwdStep fs = fwd_args(c, k, g0, ng);
         const int m = k + 1;
         if (mode == MODE_GRAD && !c->full) {
             // chunk ch >= 1 starts at qa = 1 + ch*K and keeps slices qa-1 and qa.
@@ -242,22 +327,43 @@ void record_pass(tomo_ctx* c, int mode, int g0, int ng) {
                 fs.ckstride = (int64_t)c->nchunk * 2 * N;
             }
         }
-        launch_fwd_step(prof, c->dg, c->coef, c->rcoef, fs, st);
+        if (c->strip) {
+            // slice k is gathered by the launch that computes slice k+1
+            fs.gk = k;
+            fs.gmeas = mode == MODE_GRAD ? meas_g : nullptr;
+            fs.gout = out_g;
+            fwd_launch(c, fs);
+            ++n;
+            continue;
+        }
+        fwd_launch(c, fs);
         GatherStep gs{};
         gs.u = c->hist + c->slot(m);
         gs.gstride = gstride;
         gs.k = m;
         gs.ng = ng;
-        if (mode == MODE_GRAD) {
-            gs.meas = c->meas + (int64_t)g0 * rpg;
-            gs.out = c->rr;
-            gs.part = c->rpart + (int64_t)g0 * nt;
-        } else {
-            gs.out = c->rec + (int64_t)g0 * rpg;
-        }
+        gs.meas = mode == MODE_GRAD ? meas_g : nullptr;
+        gs.out = out_g;
+        gs.part = mode == MODE_GRAD ? c->rpart + (int64_t)g0 * nt : nullptr;
         launch_gather(c->dg, gs, st);
+        n += 2;
     }
-    if (mode == MODE_FWD) return;
+    if (c->strip) {
+        GatherStep gs{};
+        gs.u = c->hist + c->slot(nt - 1);
+        gs.gstride = gstride;
+        gs.k = nt - 1;
+        gs.ng = ng;
+        gs.meas = mode == MODE_GRAD ? meas_g : nullptr;
+        gs.out = out_g;
+        launch_gather(c->dg, gs, st);
+        ++n;
+        if (mode == MODE_GRAD) {
+            launch_resid_parts(c->rr, ng, nt, (int)nch, c->rpart + (int64_t)g0 * nt, st);
+            ++n;
+        }
+    }
+    if (mode == MODE_FWD) return n;
     // ---- adjoint sweep, chunks in reverse
     cudaMemsetAsync(c->z, 0, sizeof(float) * 3 * N * ng, (cudaStream_t)st);
     cudaMemsetAsync(c->corr + (int64_t)g0 * N, 0, sizeof(float) * N * ng, (cudaStream_t)st);
@@ -268,7 +374,9 @@ void record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             if (!in_ring) {
                 if (ch == 0) {
                     launch_zero_slots(c->hist, ng, gstride, c->slot(qa - 1), c->slot(qa), N, st);
+                    ++n;
                 } else {
+                    n += 2;
                     const int64_t cks = (int64_t)c->nchunk * 2 * N;
                     launch_copy_groups(c->hist + c->slot(qa - 1), gstride, c->ckpt + ((int64_t)ch * 2 + 0) * N, cks,
                                        ng, N, st);
@@ -276,45 +384,27 @@ void record_pass(tomo_ctx* c, int mode, int g0, int ng) {
                                        N, st);
                 }
                 for (int m = qa + 1; m <= qb; ++m) {
-                    FwdStep fs{};
-                    fs.up = c->hist + c->slot(m - 2);
-                    fs.uc = c->hist + c->slot(m - 1);
-                    fs.un = c->hist + c->slot(m);
-                    fs.gstride = gstride;
-                    fs.k = m - 1;
-                    fs.g0 = g0;
-                    fs.ng = ng;
-                    launch_fwd_step(prof, c->dg, c->coef, c->rcoef, fs, st);
+                    fwd_launch(c, fwd_args(c, m - 1, g0, ng));
+                    ++n;
                 }
             }
         }
         for (int q = qb; q >= qa; --q) {
-            const int kz = (prof == TOMO_PROFILE_REF) ? q : q + 1;
-            AdjStep as{};
-            as.z2 = c->z + (int64_t)((kz + 2) % 3) * N;
-            as.z1 = c->z + (int64_t)((kz + 1) % 3) * N;
-            as.zk = c->z + (int64_t)(kz % 3) * N;
-            as.zstride = 3 * N;
-            as.uq = c->hist + c->slot(q);
-            as.ustride = gstride;
-            as.rr = c->rr + (int64_t)kz * nch;
-            as.rrstride = rpg;
-            as.corr = c->corr + (int64_t)g0 * N;
-            as.cstride = N;
-            as.k = kz;
-            as.ng = ng;
-            launch_adj_step(prof, c->dg, c->coef, as, st);
+            adj_launch(c, adj_args(c, q, g0, ng));
+            ++n;
         }
     }
+    return n;
 }
 
 tomo_status run_pass(tomo_ctx* c, int mode, int g0, int ng) {
     const auto key = std::make_tuple(mode, g0, ng);
     auto it = c->graphs.find(key);
     if (it == c->graphs.end()) {
+        TRY(autotune(c));
         cudaGraph_t graph = nullptr;
         CU(c, cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-        record_pass(c, mode, g0, ng);
+        const int64_t nk = record_pass(c, mode, g0, ng);
         const cudaError_t e = cudaStreamEndCapture(c->st, &graph);
         if (e != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
@@ -325,8 +415,10 @@ tomo_status run_pass(tomo_ctx* c, int mode, int g0, int ng) {
         cudaGraphDestroy(graph);
         if (e2 != cudaSuccess) return c->cuda(e2, "cudaGraphInstantiate");
         it = c->graphs.emplace(key, exec).first;
+        c->graph_kernels[key] = nk;
     }
     CU(c, cudaGraphLaunch(it->second, c->st));
+    c->launches += c->graph_kernels[key];
     return TOMO_OK;
 }
 
@@ -357,6 +449,7 @@ tomo_status forward_all(tomo_ctx* c, float* u_last_host) {
 tomo_status gradient_all(tomo_ctx* c) {
     const Geometry& g = c->geo;
     launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
+    ++c->launches;
     for (int g0 = 0; g0 < g.G; g0 += c->P) TRY(run_pass(c, MODE_GRAD, g0, std::min(c->P, g.G - g0)));
     return TOMO_OK;
 }
@@ -375,8 +468,10 @@ tomo_status apply_dir(tomo_ctx* c, const tomo_schedule* s, double scale) {
     if (s->normalize) {
         launch_maxabs(c->dir, c->mask, c->geo.N, c->maxabs, c->st);
         mx = c->maxabs;
+        ++c->launches;
     }
     launch_apply(c->f, c->dir, c->mask, c->geo.N, scale, mx, c->st);
+    ++c->launches;
     return TOMO_OK;
 }
 
@@ -384,6 +479,7 @@ tomo_status apply_dir(tomo_ctx* c, const tomo_schedule* s, double scale) {
 tomo_status residual_norm(tomo_ctx* c, double* out) {
     const Geometry& g = c->geo;
     launch_sum_parts(c->rpart, 1, g.G * g.nt, c->sums, c->st);
+    ++c->launches;
     CU(c, cudaMemcpyAsync(out, c->sums, sizeof(double), cudaMemcpyDeviceToHost, c->st));
     return TOMO_OK;
 }
@@ -392,6 +488,7 @@ tomo_status epsilon(tomo_ctx* c, double* out) {
     const int nb = reduce_blocks();
     launch_eps_parts(c->f, c->ftrue, c->geo.N, c->part, nb, c->st);
     launch_sum_parts(c->part, 2, nb, c->sums + 2, c->st);
+    c->launches += 2;
     double ab[2];
     CU(c, cudaMemcpyAsync(ab, c->sums + 2, sizeof ab, cudaMemcpyDeviceToHost, c->st));
     CU(c, cudaStreamSynchronize(c->st));
@@ -411,6 +508,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
     if (!std::isfinite(s)) return c->fail(TOMO_ERR_ARG, "bad schedule");
     const double sc = g.corr_scale;
     const int nb = reduce_blocks();
+    const int64_t launches0 = c->launches;
     CU(c, cudaEventRecord(c->ev0, c->st));
     double r2 = 0.0;
     if (method == TOMO_ART) {
@@ -420,6 +518,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
             launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
             TRY(run_pass(c, MODE_GRAD, gg, 1));
             launch_combine(c->corr + (int64_t)gg * N, 1, N, c->f, sc, nullptr, 1.0, c->dir, c->st);
+            c->launches += 2;
             TRY(apply_dir(c, sch, s));
         }
         TRY(residual_norm(c, &acc));
@@ -431,12 +530,14 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
         switch (method) {
         case TOMO_SIRT_CLASSIC:
             launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0, c->dir, c->st);
+            ++c->launches;
             TRY(apply_dir(c, sch, s));
             break;
         case TOMO_SIRT_SCALED:
         case TOMO_SIRT_WEIGHT:
         case TOMO_SIRT_AVG:
             launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->dir, c->st);
+            ++c->launches;
             TRY(apply_dir(c, sch, s));
             break;
         case TOMO_SIRT_NORM: {
@@ -444,6 +545,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
             launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->tmp, c->st);
             launch_group_dev_norm(c->corr, G, N, c->f, sc, c->tmp, c->part, nb, c->st);
             launch_sum_parts(c->part, G, nb, c->sums, c->st);
+            c->launches += 3;
             std::vector<double> d2(G);
             CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
             CU(c, cudaStreamSynchronize(c->st));
@@ -453,6 +555,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
             for (int gg = 0; gg < G; ++gg) w[gg] /= W;
             CU(c, cudaMemcpyAsync(c->sums, w.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
             launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
+            ++c->launches;
             TRY(apply_dir(c, sch, s));
             CU(c, cudaStreamSynchronize(c->st));   // w lives on the host stack
             break;
@@ -463,6 +566,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
             launch_avgw_norm(c->corr, G, N, c->f, c->mask, sc, s, c->tmp, c->part, nb, c->st);
             launch_sum_parts(c->part, G, nb, c->sums, c->st);
             launch_avgw_apply(c->corr, G, N, c->f, c->mask, sc, s, c->sums, c->st);
+            c->launches += 4;
             break;
         }
         default:
@@ -482,6 +586,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
         stats->scale = s;
         stats->seconds = ms * 1e-3;
         stats->cell_updates = 2.0 * (double)G * (double)(g.nt - 2) * (double)N;
+        stats->kernel_launches = (double)(c->launches - launches0);
     }
     return TOMO_OK;
 }
@@ -722,6 +827,32 @@ tomo_status tomo_iterate_device(tomo_ctx* c, int32_t method, const tomo_schedule
     if (d_f_true) CU(c, cudaMemcpyAsync(c->ftrue, d_f_true, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
     TRY(iterate_core(c, method, sched, iter, d_f_true != nullptr, stats));
     CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    return TOMO_OK;
+}
+
+tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* ms_per_launch,
+                             double* bytes_per_launch) {
+    if (!c || (which != 0 && which != 1) || steps < 1 || !ms_per_launch)
+        return c ? c->fail(TOMO_ERR_ARG, "bad tomo_time_kernel arguments") : TOMO_ERR_ARG;
+    CU(c, cudaSetDevice(c->dev));
+    const Geometry& g = c->geo;
+    const int nt = g.nt, ng = c->P, prof = g.cfg.profile;
+    const int64_t N = g.N;
+    steps = std::min(steps, nt - 4);
+    const int k0 = std::max(1, (nt - steps) / 2);
+    launch_coef(prof, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
+    CU(c, cudaEventRecord(c->ev0, c->st));
+    for (int t = 0; t < steps; ++t) {
+        if (which == 0) fwd_launch(c, fwd_args(c, k0 + t, 0, ng));
+        else adj_launch(c, adj_args(c, k0 + steps - 1 - t, 0, ng));
+    }
+    CU(c, cudaEventRecord(c->ev1, c->st));
+    CU(c, cudaEventSynchronize(c->ev1));
+    CU(c, cudaGetLastError());
+    float ms = 0.f;
+    CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    *ms_per_launch = (double)ms / steps;
+    if (bytes_per_launch) *bytes_per_launch = (which == 0 ? 16.0 : 20.0) * (double)ng * (double)N;
     return TOMO_OK;
 }
 

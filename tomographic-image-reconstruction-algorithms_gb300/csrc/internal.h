@@ -85,6 +85,10 @@ struct FwdStep {
     int k;             // computing slice k+1
     int g0;            // global index of pass-group 0
     int ng;            // groups in the pass
+    // fused sensor gather of slice k (strip kernels only; gk < 2: none)
+    int gk = -1;
+    const float* gmeas = nullptr;   // measured records of pass-group 0, or null (simulate)
+    float* gout = nullptr;          // records / residual of pass-group 0
 };
 
 struct AdjStep {
@@ -146,5 +150,11 @@ void launch_apply(float* f, const float* dir, const uint8_t* mask, int64_t N, do
 void launch_eps_parts(const float* f, const float* fo, int64_t N, double* part, int nb, void* stream);
 
 int reduce_blocks();  // number of partial blocks the reductions use
+
+// warp-strip step kernels (strip.cu): CFG profile, nx % 4 == 0; rows per warp in {2,4,8,16,32}
+bool strip_supported(const DevGeo& g, int profile);
+void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& s, void* stream);
+void launch_adj_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& s, void* stream);
+void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, void* stream);
 
 }  // namespace tomo

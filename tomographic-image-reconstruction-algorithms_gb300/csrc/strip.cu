@@ -1,0 +1,268 @@
+// strip.cu -- warp-strip step kernels of the synthetic-workload (CFG) physics.
+//
+// Each warp owns a 128-cell-wide strip of R consecutive rows of one group: a
+// lane holds four consecutive cells and moves them with 128-bit loads and
+// stores; the rows above and below roll through registers, east and west
+// neighbours come from warp shuffles (plus one scalar load at each end of the
+// strip).  Per cell-update the forward step then touches u(k) once, u(k-1) once,
+// the coefficient once and writes u(k+1) once -- the 16 bytes the update needs
+// -- with a handful of instructions.  The adjoint step rolls z(k+1), the
+// coefficient and the forward slice u(q) the same way and keeps the
+// correlation update to one 128-bit read-modify-write per four cells.
+//
+// The forward launch also carries the sensor gather of slice k in one extra
+// block per group (it reads slice k, which is complete), replacing a separate
+// launch per step.  Same arithmetic, operand order and results as the per-cell
+// kernels in kernels.cu.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "internal.h"
+
+namespace tomo {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int STRIP = 128;     // cells per warp strip
+constexpr int WARPS = 4;       // warps per block (stacked in y)
+
+__device__ __forceinline__ float4 ld4(const float* __restrict__ p, int64_t off, bool ok) {
+    return ok ? *reinterpret_cast<const float4*>(p + off) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ float sponge(int i, int j, int nx, int ny, int w, float smax) {
+    const int dd = min(min(i, j), min(nx - 1 - i, ny - 1 - j));
+    if (dd >= w) return 1.f;
+    const float x = (float)(w - dd) / (float)w;
+    return 1.f - smax * x * x;
+}
+
+// West neighbour of element 0 and east neighbour of element 3 of each lane.
+__device__ __forceinline__ void we(const float4& v, const float* __restrict__ row, int lane, int x0, int nx,
+                                   float& west, float& east) {
+    west = __shfl_up_sync(FULL, v.w, 1);
+    east = __shfl_down_sync(FULL, v.x, 1);
+    if (lane == 0) west = x0 > 0 ? row[x0 - 1] : 0.f;
+    if (lane == 31) east = x0 + STRIP < nx ? row[x0 + STRIP] : 0.f;
+}
+
+// ---------------------------------------------------------------------------
+template <int R>
+__global__ void __launch_bounds__(WARPS * 32) k_fwd_strip(DevGeo g, const float* __restrict__ coef, FwdStep s) {
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    if (blockIdx.y == gridDim.y - 1) {
+        // sensor gather of slice k (k >= 2), one block per group
+        if (blockIdx.x != 0 || s.gk < 2) return;
+        const float* u = s.uc + gl * s.gstride;
+        const int64_t base = ((int64_t)gl * g.nt + s.gk) * g.nch;
+        for (int c = threadIdx.x; c < g.nch; c += blockDim.x) {
+            const int cell = g.rcv[c];
+            const float v = cell >= 0 ? u[cell] : 0.f;
+            s.gout[base + c] = s.gmeas ? (cell >= 0 ? s.gmeas[base + c] - v : 0.f) : v;
+        }
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * STRIP;
+    const int i = x0 + 4 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    const bool act = i < nx;
+    const float* uc = s.uc + gl * s.gstride;
+    const float* up = s.up + gl * s.gstride;
+    float* un = s.un + gl * s.gstride;
+    float* ck = s.ck ? s.ck + gl * s.ckstride : nullptr;
+    const bool edge_x = x0 < g.sponge_w || x0 + STRIP > nx - g.sponge_w;
+    const bool src = s.k < g.n_src_steps;
+    const int32_t* em = g.emit + (int64_t)(s.g0 + gl) * g.gs;
+    const float a = src ? g.src[s.k] : 0.f;
+    float4 rm = ld4(uc, (int64_t)(y0 - 1) * nx + i, act && y0 > 0);
+    float4 r0 = ld4(uc, (int64_t)y0 * nx + i, act);
+#pragma unroll 4
+    for (int r = 0; r < R; ++r) {
+        const int j = y0 + r;
+        if (j >= ny) break;
+        const int64_t row = (int64_t)j * nx;
+        const float4 rp = ld4(uc, row + nx + i, act && j + 1 < ny);
+        const float4 p = ld4(up, row + i, act);
+        const float4 c = ld4(coef, row + i, act);
+        float w, e;
+        we(r0, uc + row, lane, x0, nx, w, e);
+        float4 v;
+        v.x = (2.f * r0.x - p.x) + c.x * ((((r0.y + w) + rm.x) + rp.x) - 4.f * r0.x);
+        v.y = (2.f * r0.y - p.y) + c.y * ((((r0.z + r0.x) + rm.y) + rp.y) - 4.f * r0.y);
+        v.z = (2.f * r0.z - p.z) + c.z * ((((r0.w + r0.y) + rm.z) + rp.z) - 4.f * r0.z);
+        v.w = (2.f * r0.w - p.w) + c.w * ((((e + r0.z) + rm.w) + rp.w) - 4.f * r0.w);
+        if (edge_x || j < g.sponge_w || j >= ny - g.sponge_w) {
+            v.x *= sponge(i, j, nx, ny, g.sponge_w, g.sponge_max);
+            v.y *= sponge(i + 1, j, nx, ny, g.sponge_w, g.sponge_max);
+            v.z *= sponge(i + 2, j, nx, ny, g.sponge_w, g.sponge_max);
+            v.w *= sponge(i + 3, j, nx, ny, g.sponge_w, g.sponge_max);
+        }
+        if (src) {
+            const int64_t q0 = row + i;
+            for (int t = 0; t < g.gs; ++t) {
+                const int64_t d = (int64_t)em[t] - q0;
+                if (d == 0) v.x += a;
+                else if (d == 1) v.y += a;
+                else if (d == 2) v.z += a;
+                else if (d == 3) v.w += a;
+            }
+        }
+        if (act) {
+            *reinterpret_cast<float4*>(un + row + i) = v;
+            if (ck) *reinterpret_cast<float4*>(ck + row + i) = v;
+        }
+        rm = r0;
+        r0 = rp;
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <int R>
+__global__ void __launch_bounds__(WARPS * 32) k_adj_strip(DevGeo g, const float* __restrict__ coef, AdjStep s) {
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * STRIP;
+    const int i = x0 + 4 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    const bool act = i < nx;
+    const float* z1 = s.z1 + gl * s.zstride;
+    const float* z2 = s.z2 + gl * s.zstride;
+    float* zk = s.zk + gl * s.zstride;
+    const float* u = s.uq + gl * s.ustride;
+    const float* rr = s.rr + gl * s.rrstride;
+    float* corr = s.corr + gl * s.cstride;
+    const bool edge_x = x0 < g.sponge_w || x0 + STRIP > nx - g.sponge_w;
+    // rolling rows: z1, coef*z1 and u
+    float4 zm = ld4(z1, (int64_t)(y0 - 1) * nx + i, act && y0 > 0);
+    float4 cm = ld4(coef, (int64_t)(y0 - 1) * nx + i, act && y0 > 0);
+    float4 z0 = ld4(z1, (int64_t)y0 * nx + i, act);
+    float4 c0 = ld4(coef, (int64_t)y0 * nx + i, act);
+    float4 um = ld4(u, (int64_t)(y0 - 1) * nx + i, act && y0 > 0);
+    float4 u0 = ld4(u, (int64_t)y0 * nx + i, act);
+#pragma unroll 2
+    for (int r = 0; r < R; ++r) {
+        const int j = y0 + r;
+        if (j >= ny) break;
+        const int64_t row = (int64_t)j * nx;
+        const bool has_next = act && j + 1 < ny;
+        const float4 zp = ld4(z1, row + nx + i, has_next);
+        const float4 cp = ld4(coef, row + nx + i, has_next);
+        const float4 uq = ld4(u, row + nx + i, has_next);
+        const float4 zz = ld4(z2, row + i, act);
+        // coefficient-weighted neighbours of z(k+1): c*z at west/east via shuffles
+        const float4 cz0 = make_float4(c0.x * z0.x, c0.y * z0.y, c0.z * z0.z, c0.w * z0.w);
+        float czw = __shfl_up_sync(FULL, cz0.w, 1), cze = __shfl_down_sync(FULL, cz0.x, 1);
+        if (lane == 0) czw = x0 > 0 ? coef[row + x0 - 1] * z1[row + x0 - 1] : 0.f;
+        if (lane == 31) cze = x0 + STRIP < nx ? coef[row + x0 + STRIP] * z1[row + x0 + STRIP] : 0.f;
+        float v[4];
+        const float czs[4] = {cm.x * zm.x, cm.y * zm.y, cm.z * zm.z, cm.w * zm.w};
+        const float czn[4] = {cp.x * zp.x, cp.y * zp.y, cp.z * zp.z, cp.w * zp.w};
+        const float cze4[4] = {cz0.y, cz0.z, cz0.w, cze};
+        const float czw4[4] = {czw, cz0.x, cz0.y, cz0.z};
+        const float zc[4] = {z0.x, z0.y, z0.z, z0.w};
+        const float cc[4] = {c0.x, c0.y, c0.z, c0.w};
+        const float z2v[4] = {zz.x, zz.y, zz.z, zz.w};
+        const bool near_y = j < g.sponge_w || j >= ny - g.sponge_w;
+        int4 rid = act ? *reinterpret_cast<const int4*>(g.rid + row + i) : make_int4(-1, -1, -1, -1);
+        const int rids[4] = {rid.x, rid.y, rid.z, rid.w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const float lz = (((cze4[t] + czw4[t]) + czs[t]) + czn[t]) - 4.f * cc[t] * zc[t];
+            const float inj = rids[t] >= 0 ? rr[rids[t]] : 0.f;
+            float d = 1.f;
+            if (edge_x || near_y) d = sponge(i + t, j, nx, ny, g.sponge_w, g.sponge_max);
+            v[t] = d * ((2.f * zc[t] - z2v[t]) + lz + inj);
+        }
+        // Laplacian of the forward slice (zero outside the grid)
+        float uw, ue;
+        we(u0, u + row, lane, x0, nx, uw, ue);
+        const float uus[4] = {um.x, um.y, um.z, um.w};
+        const float uun[4] = {uq.x, uq.y, uq.z, uq.w};
+        const float uc4[4] = {u0.x, u0.y, u0.z, u0.w};
+        const float uue[4] = {u0.y, u0.z, u0.w, ue};
+        const float uuw[4] = {uw, u0.x, u0.y, u0.z};
+        if (act) {
+            float4 cr = *reinterpret_cast<const float4*>(corr + row + i);
+            float lu[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) lu[t] = (((uue[t] + uuw[t]) + uus[t]) + uun[t]) - 4.f * uc4[t];
+            cr.x += v[0] * lu[0];
+            cr.y += v[1] * lu[1];
+            cr.z += v[2] * lu[2];
+            cr.w += v[3] * lu[3];
+            *reinterpret_cast<float4*>(corr + row + i) = cr;
+            *reinterpret_cast<float4*>(zk + row + i) = make_float4(v[0], v[1], v[2], v[3]);
+        }
+        zm = z0; z0 = zp;
+        cm = c0; c0 = cp;
+        um = u0; u0 = uq;
+    }
+}
+
+// part[(g0+gl)*nt + k] = sum_c rr(gl, k, c)^2, one block per (k, group), fixed order.
+__global__ void __launch_bounds__(256) k_resid_parts(const float* __restrict__ rr, int nt, int nch, double* part) {
+    const int k = blockIdx.x, gl = blockIdx.y;
+    const float* r = rr + ((int64_t)gl * nt + k) * nch;
+    double acc = 0.0;
+    for (int c = threadIdx.x; c < nch; c += 256) acc += (double)r[c] * (double)r[c];
+    __shared__ double red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(int64_t)gl * nt + k] = red[0];
+}
+
+template <int R>
+void fwd_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    dim3 grid((g.nx + STRIP - 1) / STRIP, (g.ny + rows_per_block - 1) / rows_per_block + 1, s.ng);
+    k_fwd_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+}
+
+template <int R>
+void adj_strip(const DevGeo& g, const float* coef, const AdjStep& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    dim3 grid((g.nx + STRIP - 1) / STRIP, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
+    k_adj_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+}
+
+}  // namespace
+
+void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, void* stream) {
+    k_resid_parts<<<dim3(nt, ng), 256, 0, (cudaStream_t)stream>>>(rr, nt, nch, part);
+}
+
+bool strip_supported(const DevGeo& g, int profile) { return profile == TOMO_PROFILE_CFG && g.nx % 4 == 0; }
+
+void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& s, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (rows) {
+    case 2: fwd_strip<2>(g, coef, s, st); break;
+    case 4: fwd_strip<4>(g, coef, s, st); break;
+    case 16: fwd_strip<16>(g, coef, s, st); break;
+    case 32: fwd_strip<32>(g, coef, s, st); break;
+    default: fwd_strip<8>(g, coef, s, st); break;
+    }
+}
+
+void launch_adj_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& s, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (rows) {
+    case 2: adj_strip<2>(g, coef, s, st); break;
+    case 4: adj_strip<4>(g, coef, s, st); break;
+    case 16: adj_strip<16>(g, coef, s, st); break;
+    case 32: adj_strip<32>(g, coef, s, st); break;
+    default: adj_strip<8>(g, coef, s, st); break;
+    }
+}
+
+}  // namespace tomo

@@ -60,7 +60,7 @@ class Schedule(C.Structure):
 class IterStats(C.Structure):
     _fields_ = [
         ("epsilon", C.c_double), ("resid_norm2", C.c_double), ("scale", C.c_double),
-        ("seconds", C.c_double), ("cell_updates", C.c_double),
+        ("seconds", C.c_double), ("cell_updates", C.c_double), ("kernel_launches", C.c_double),
     ]
 
 
@@ -158,6 +158,7 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_forward_device": (i32, [vp, vp, vp]),
         "tomo_iterate_device": (i32, [vp, i32, C.POINTER(Schedule), i32, vp, vp, vp, C.POINTER(IterStats)]),
         "tomo_synchronize": (i32, [vp]),
+        "tomo_time_kernel": (i32, [vp, i32, i32, DP, DP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -294,6 +295,12 @@ class Context:
                                               C.c_void_p(d_rec or None), C.c_void_p(d_ftrue or None),
                                               C.byref(stats)))
         return stats
+
+    def time_kernel(self, which: int, steps: int):
+        """(ms per launch, algorithmic bytes per launch) of the forward (0) or adjoint (1) step."""
+        ms, by = C.c_double(), C.c_double()
+        self._check(lib().tomo_time_kernel(self.h, which, steps, C.byref(ms), C.byref(by)))
+        return ms.value, by.value
 
     def synchronize(self):
         self._check(lib().tomo_synchronize(self.h))
