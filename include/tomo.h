@@ -216,6 +216,23 @@ tomo_status tomo_synchronize(tomo_ctx* ctx);
 tomo_status tomo_time_kernel(tomo_ctx* ctx, int32_t which, int32_t steps,
                              double* ms_per_launch, double* bytes_per_launch);
 
+/* Forward solve without any device allocation (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc: applications whose own
+ * pool allocator owns all device memory, or latency-bound loops where
+ * cudaMalloc/cudaFree would synchronise the device.  d_f (nx*ny) and d_records
+ * (G*nt*n_channels, the tomo_forward layout) are caller-owned device buffers on
+ * the current device; work is enqueued on `stream` (NULL: legacy default) and
+ * the records are valid once it completes.  The wavefield scratch lives in a
+ * fixed file-scope device array of about 5.1 MiB that each GPU loading the
+ * library holds until exit, so problems are limited to 512*512 cells, 2048
+ * record channels, 2048 groups, 4096 emitters and 16384 time steps; larger ones
+ * return TOMO_ERR_ARG with a one-line reason on stderr.  The first call on a
+ * device looks the array's address up (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race. */
+tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float* d_f, float* d_records,
+                                 void* stream);
+
 #ifdef __cplusplus
 }
 #endif

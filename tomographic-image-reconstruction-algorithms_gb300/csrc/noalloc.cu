@@ -1,0 +1,154 @@
+// noalloc.cu -- forward solve into caller-owned device buffers with no device
+// allocation at all (tomo_forward_noalloc in include/tomo.h).
+//
+// Why it exists: tomo_create sizes and cudaMallocs a context.  Some callers
+// cannot do that -- a host application that hands every byte of device memory
+// to its own pool allocator and forbids raw cudaMalloc, or a latency-bound loop
+// where cudaMalloc/cudaFree would synchronise the device and stall its other
+// streams.  They pass their own input and output buffers; the wavefield
+// scratch this solve needs lives in the file-scope array below instead.
+//
+// The scratch array g_scratch is a fixed kNoallocScratchBytes (about 5.1 MiB)
+// that every GPU loading this library holds until the process exits.  It holds,
+// for one emitter group at a time, the three forward time slots, the two
+// coefficient fields and the geometry tables, so a call accepts grids of up to
+// kNoallocMaxCells cells (512 x 512), kNoallocMaxChannels record channels,
+// kNoallocMaxGroups groups, kNoallocMaxEmitters emitters and kNoallocMaxSteps
+// time steps, and rejects anything larger with TOMO_ERR_ARG.
+//
+// In host code g_scratch names a host-side stand-in, not device memory; the
+// device address is looked up once per device with cudaGetSymbolAddress (the
+// first call on a device does it, with that device current -- make that first
+// call before any stream capture) and that pointer is what the kernels get.
+//
+// All calls share the one array and it keeps the last call's contents: each
+// call zeroes the two initial time slots it starts from and the output records,
+// and rewrites everything else before reading it.  Calls that overlap on the
+// GPU (concurrent streams, or threads, on the same device) race on the array.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "internal.h"
+
+namespace tomo {
+namespace {
+
+constexpr int64_t kNoallocMaxCells = 512 * 512;
+constexpr int kNoallocMaxChannels = 2048;
+constexpr int kNoallocMaxGroups = 2048;
+constexpr int kNoallocMaxEmitters = 4096;
+constexpr int kNoallocMaxSteps = 16384;
+
+// float region: 3 time slots + coefficient + edge coefficient + source table
+constexpr int64_t kFloats = 5 * kNoallocMaxCells + kNoallocMaxSteps;
+// int region: receiver cells + emitter cells + emission boxes
+constexpr int64_t kInts = kNoallocMaxChannels + kNoallocMaxEmitters + 4 * kNoallocMaxGroups;
+constexpr int64_t kNoallocScratchBytes = 4 * (kFloats + kInts);
+
+static __device__ __align__(256) unsigned char g_scratch[kNoallocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_addr[kMaxDevices] = {};
+// Failures are returned as a status and explained in one line on stderr.
+tomo_status fail(tomo_status s, const std::string& why) {
+    std::fprintf(stderr, "tomo_forward_noalloc: %s\n", why.c_str());
+    return s;
+}
+
+tomo_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(TOMO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Device address of g_scratch on the current device (looked up once per device).
+tomo_status scratch_address(unsigned char** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return fail(TOMO_ERR_ARG, "device ordinal too large");
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess || !p) return cuda_fail(e, "cudaGetSymbolAddress(g_scratch)");
+        g_addr[dev] = p;
+    }
+    *out = (unsigned char*)g_addr[dev];
+    return TOMO_OK;
+}
+
+}  // namespace
+}  // namespace tomo
+
+using namespace tomo;
+
+extern "C" tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float* d_f, float* d_records,
+                                            void* stream) {
+    if (!cfg || !d_f || !d_records) return fail(TOMO_ERR_ARG, "NULL argument");
+    Geometry geo;
+    std::string why;
+    tomo_status s = build_geometry(*cfg, geo, why);
+    if (s != TOMO_OK) return fail(s, why);
+    if (geo.N > kNoallocMaxCells || geo.nch > kNoallocMaxChannels || geo.G > kNoallocMaxGroups ||
+        (int64_t)geo.G * geo.gs > kNoallocMaxEmitters || geo.nt > kNoallocMaxSteps)
+        return fail(TOMO_ERR_ARG, "problem exceeds the allocation-free limits (cells <= 262144, channels <= 2048, "
+                                  "groups <= 2048, emitters <= 4096, steps <= 16384)");
+    unsigned char* base = nullptr;
+    if ((s = scratch_address(&base)) != TOMO_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t N = geo.N, nt = geo.nt, nch = geo.nch;
+    float* slots = (float*)base;                       // 3 time slots
+    float* coef = slots + 3 * kNoallocMaxCells;
+    float* rcoef = coef + kNoallocMaxCells;
+    float* src = rcoef + kNoallocMaxCells;
+    int32_t* rcv = (int32_t*)(src + kNoallocMaxSteps);
+    int32_t* emit = rcv + kNoallocMaxChannels;
+    int32_t* box = emit + kNoallocMaxEmitters;
+    cudaError_t e;
+#define NA_CU(x)                                     \
+    do {                                             \
+        if ((e = (x)) != cudaSuccess) return cuda_fail(e, #x); \
+    } while (0)
+    NA_CU(cudaMemcpyAsync(src, geo.src.data(), sizeof(float) * nt, cudaMemcpyHostToDevice, st));
+    NA_CU(cudaMemcpyAsync(rcv, geo.rcv.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, st));
+    if (geo.ref) NA_CU(cudaMemcpyAsync(box, geo.box.data(), sizeof(int32_t) * 4 * geo.G, cudaMemcpyHostToDevice, st));
+    else NA_CU(cudaMemcpyAsync(emit, geo.emit.data(), sizeof(int32_t) * geo.G * geo.gs, cudaMemcpyHostToDevice, st));
+    NA_CU(cudaMemsetAsync(d_records, 0, sizeof(float) * (size_t)geo.G * nt * nch, st));
+    DevGeo dg{};
+    dg.nx = geo.nx; dg.ny = geo.ny; dg.nt = geo.nt; dg.nch = geo.nch;
+    dg.lo = geo.lo; dg.hi = geo.hi; dg.gs = geo.gs;
+    dg.sponge_w = cfg->sponge_width; dg.sponge_max = cfg->sponge_max;
+    dg.box = box; dg.emit = emit; dg.rcv = rcv; dg.rid = nullptr; dg.src = src;
+    dg.n_src_steps = geo.n_src_steps;
+    const int prof = cfg->profile;
+    launch_coef(prof, d_f, coef, rcoef, N, cfg->courant, st);
+    auto slot = [&](int k) { return slots + (int64_t)(k % 3) * N; };
+    for (int g = 0; g < geo.G; ++g) {
+        launch_zero_slots(slots, 1, 3 * N, 0, N, N, st);   // u(0) = u(1) = 0
+        for (int k = 1; k <= geo.nt - 2; ++k) {
+            FwdStep fs{};
+            fs.up = slot(k - 1);
+            fs.uc = slot(k);
+            fs.un = slot(k + 1);
+            fs.gstride = 3 * N;
+            fs.k = k;
+            fs.g0 = g;
+            fs.ng = 1;
+            launch_fwd_step(prof, dg, coef, rcoef, fs, st);
+            GatherStep gs{};
+            gs.u = slot(k + 1);
+            gs.gstride = 3 * N;
+            gs.out = d_records + (int64_t)g * nt * nch;
+            gs.k = k + 1;
+            gs.ng = 1;
+            launch_gather(dg, gs, st);
+        }
+    }
+    NA_CU(cudaGetLastError());
+#undef NA_CU
+    return TOMO_OK;
+}

@@ -159,6 +159,7 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_iterate_device": (i32, [vp, i32, C.POINTER(Schedule), i32, vp, vp, vp, C.POINTER(IterStats)]),
         "tomo_synchronize": (i32, [vp]),
         "tomo_time_kernel": (i32, [vp, i32, i32, DP, DP]),
+        "tomo_forward_noalloc": (i32, [C.POINTER(Config), vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
