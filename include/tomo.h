@@ -210,8 +210,9 @@ tomo_status tomo_synchronize(tomo_ctx* ctx);
 /* Profiling hook (no reference counterpart): runs `steps` consecutive time steps
  * of one hot kernel for the first pass's groups on the context stream, bracketed
  * by CUDA events, after at least one tomo_iterate.  which: 0 forward step,
- * 1 adjoint step.  Returns the mean duration of one launch and the algorithmic
- * bytes one launch moves (16 B forward / 20 B adjoint per cell-update).
+ * 1 adjoint step.  Returns the mean duration of one time step (kernels that
+ * advance two steps per launch count as two) and the algorithmic bytes of one
+ * step (16 B forward / 20 B adjoint per cell-update).
  * Clobbers the iteration's scratch state (the next tomo_iterate rebuilds it). */
 tomo_status tomo_time_kernel(tomo_ctx* ctx, int32_t which, int32_t steps,
                              double* ms_per_launch, double* bytes_per_launch);

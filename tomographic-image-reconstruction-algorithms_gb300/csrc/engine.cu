@@ -65,7 +65,10 @@ struct tomo_ctx {
     std::map<std::tuple<int, int, int>, int64_t> graph_kernels;   // kernel nodes per graph
     int64_t launches = 0;                                          // kernels issued since reset
     bool strip = false;          // warp-strip kernels (CFG, nx % 4 == 0)
-    int rows_fwd = 8, rows_adj = 8;
+    int rows_fwd = 8, rows_adj = 8, adj_variant = 0;
+    bool adj_pair = false;       // two adjoint steps per launch (strip kernels)
+    int rows_adj2 = 8;
+    static constexpr int ZR = 4; // adjoint ring slots
     bool tuned = false;
     std::vector<void*> allocs;
 
@@ -131,7 +134,7 @@ void fwd_launch(tomo_ctx* c, const FwdStep& fs) {
 }
 
 void adj_launch(tomo_ctx* c, const AdjStep& as) {
-    if (c->strip) launch_adj_strip(c->rows_adj, c->dg, c->coef, as, c->st);
+    if (c->strip) launch_adj_strip(c->rows_adj, c->adj_variant, c->dg, c->coef, as, c->st);
     else launch_adj_step(c->geo.cfg.profile, c->dg, c->coef, as, c->st);
 }
 
@@ -150,11 +153,12 @@ FwdStep fwd_args(tomo_ctx* c, int k, int g0, int ng) {
 AdjStep adj_args(tomo_ctx* c, int q, int g0, int ng) {
     const int64_t N = c->geo.N;
     const int kz = (c->geo.cfg.profile == TOMO_PROFILE_REF) ? q : q + 1;
+    const int zr = tomo_ctx::ZR;
     AdjStep as{};
-    as.z2 = c->z + (int64_t)((kz + 2) % 3) * N;
-    as.z1 = c->z + (int64_t)((kz + 1) % 3) * N;
-    as.zk = c->z + (int64_t)(kz % 3) * N;
-    as.zstride = 3 * N;
+    as.z2 = c->z + (int64_t)((kz + 2) % zr) * N;
+    as.z1 = c->z + (int64_t)((kz + 1) % zr) * N;
+    as.zk = c->z + (int64_t)(kz % zr) * N;
+    as.zstride = zr * N;
     as.uq = c->hist + c->slot(q);
     as.ustride = (int64_t)c->S * N;
     as.rr = c->rr + (int64_t)kz * c->geo.nch;
@@ -172,29 +176,45 @@ tomo_status autotune(tomo_ctx* c) {
     if (c->tuned || !c->strip) { c->tuned = true; return TOMO_OK; }
     c->tuned = true;
     if (const char* e = std::getenv("TOMO_STRIP_ROWS")) {
-        c->rows_fwd = c->rows_adj = std::atoi(e);
+        c->rows_fwd = c->rows_adj = c->rows_adj2 = std::atoi(e);
+        if (const char* v = std::getenv("TOMO_ADJ_VARIANT")) c->adj_variant = std::atoi(v);
+        if (const char* v = std::getenv("TOMO_ADJ_PAIR")) c->adj_pair = std::atoi(v) != 0;
         return TOMO_OK;
     }
     const int cands[5] = {2, 4, 8, 16, 32};
     const int nt = c->geo.nt, ng = c->P, reps = 6;
     const int k0 = std::max(1, nt / 2 - reps);
     float best_f = 1e30f, best_a = 1e30f;
+    // forward: rows per warp; adjoint: rows per warp x register/unroll variant
     for (int rows : cands) {
         if (rows > 4 * c->geo.ny) continue;
-        for (int which = 0; which < 2; ++which) {
+        for (int which = 0; which < 5; ++which) {
             float ms = 0.f;
             for (int pass = 0; pass < 2; ++pass) {   // first pass warms up
                 CU(c, cudaEventRecord(c->ev0, c->st));
                 for (int t = 0; t < reps; ++t) {
                     if (which == 0) launch_fwd_strip(rows, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), c->st);
-                    else launch_adj_strip(rows, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, ng), c->st);
+                    else launch_adj_strip(rows, which - 1, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, ng), c->st);
                 }
                 CU(c, cudaEventRecord(c->ev1, c->st));
                 CU(c, cudaEventSynchronize(c->ev1));
                 CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
             }
             if (which == 0 && ms < best_f) { best_f = ms; c->rows_fwd = rows; }
-            if (which == 1 && ms < best_a) { best_a = ms; c->rows_adj = rows; }
+            if (which > 0 && ms < best_a) { best_a = ms; c->rows_adj = rows; c->adj_variant = which - 1; }
+        }
+        if (rows >= 4) {   // two steps per launch: reps/2 launches cover the same steps
+            float ms = 0.f;
+            for (int pass = 0; pass < 2; ++pass) {
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                for (int t = 0; t < reps; t += 2)
+                    launch_adj2_strip(rows, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, ng),
+                                      adj_args(c, k0 + reps - t - 1, 0, ng), c->st);
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            }
+            if (ms < best_a) { best_a = ms; c->rows_adj2 = rows; c->adj_pair = true; }
         }
     }
     CU(c, cudaGetLastError());
@@ -256,7 +276,7 @@ tomo_status create_buffers(tomo_ctx* c) {
     TRY(c->alloc(&c->dir, N, "dir"));
     TRY(c->alloc(&c->tmp, N, "tmp"));
     TRY(c->alloc(&c->hist, P * c->S * N, "forward slots"));
-    TRY(c->alloc(&c->z, P * 3 * N, "adjoint slots"));
+    TRY(c->alloc(&c->z, P * tomo_ctx::ZR * N, "adjoint slots"));
     if (!c->full) TRY(c->alloc(&c->ckpt, P * c->nchunk * 2 * N, "checkpoints"));
     TRY(c->alloc(&c->corr, G * N, "correlation"));
     TRY(c->alloc(&c->meas, G * nt * nch, "measured records"));
@@ -294,7 +314,7 @@ tomo_status create_buffers(tomo_ctx* c) {
     d.n_src_steps = g.n_src_steps;
     c->strip = strip_supported(d, g.cfg.profile) && !std::getenv("TOMO_NO_STRIP");
     CU(c, cudaMemsetAsync(c->hist, 0, sizeof(float) * (size_t)P * c->S * N, c->st));
-    CU(c, cudaMemsetAsync(c->z, 0, sizeof(float) * (size_t)P * 3 * N, c->st));
+    CU(c, cudaMemsetAsync(c->z, 0, sizeof(float) * (size_t)P * tomo_ctx::ZR * N, c->st));
     CU(c, cudaMemsetAsync(c->corr, 0, sizeof(float) * (size_t)G * N, c->st));
     CU(c, cudaStreamSynchronize(c->st));
     return TOMO_OK;
@@ -365,7 +385,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     }
     if (mode == MODE_FWD) return n;
     // ---- adjoint sweep, chunks in reverse
-    cudaMemsetAsync(c->z, 0, sizeof(float) * 3 * N * ng, (cudaStream_t)st);
+    cudaMemsetAsync(c->z, 0, sizeof(float) * tomo_ctx::ZR * N * ng, (cudaStream_t)st);
     cudaMemsetAsync(c->corr + (int64_t)g0 * N, 0, sizeof(float) * N * ng, (cudaStream_t)st);
     for (int ch = c->nchunk - 1; ch >= 0; --ch) {
         const int qa = 1 + ch * K, qb = std::min(qa + K - 1, nt - 2);
@@ -389,8 +409,14 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
                 }
             }
         }
-        for (int q = qb; q >= qa; --q) {
-            adj_launch(c, adj_args(c, q, g0, ng));
+        for (int q = qb; q >= qa;) {
+            if (c->adj_pair && q - 1 >= qa) {
+                launch_adj2_strip(c->rows_adj2, c->dg, c->coef, adj_args(c, q, g0, ng), adj_args(c, q - 1, g0, ng), st);
+                q -= 2;
+            } else {
+                adj_launch(c, adj_args(c, q, g0, ng));
+                q -= 1;
+            }
             ++n;
         }
     }
@@ -839,12 +865,22 @@ tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* 
     const int nt = g.nt, ng = c->P, prof = g.cfg.profile;
     const int64_t N = g.N;
     steps = std::min(steps, nt - 4);
-    const int k0 = std::max(1, (nt - steps) / 2);
+    const int k0 = std::max(2, (nt - steps) / 2);
     launch_coef(prof, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
+    TRY(autotune(c));
     CU(c, cudaEventRecord(c->ev0, c->st));
-    for (int t = 0; t < steps; ++t) {
-        if (which == 0) fwd_launch(c, fwd_args(c, k0 + t, 0, ng));
-        else adj_launch(c, adj_args(c, k0 + steps - 1 - t, 0, ng));
+    for (int t = 0; t < steps;) {
+        if (which == 0) {
+            fwd_launch(c, fwd_args(c, k0 + t, 0, ng));
+            t += 1;
+        } else if (c->adj_pair && t + 1 < steps) {
+            const int q = k0 + steps - 1 - t;
+            launch_adj2_strip(c->rows_adj2, c->dg, c->coef, adj_args(c, q, 0, ng), adj_args(c, q - 1, 0, ng), c->st);
+            t += 2;
+        } else {
+            adj_launch(c, adj_args(c, k0 + steps - 1 - t, 0, ng));
+            t += 1;
+        }
     }
     CU(c, cudaEventRecord(c->ev1, c->st));
     CU(c, cudaEventSynchronize(c->ev1));

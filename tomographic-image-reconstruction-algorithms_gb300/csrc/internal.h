@@ -154,7 +154,13 @@ int reduce_blocks();  // number of partial blocks the reductions use
 // warp-strip step kernels (strip.cu): CFG profile, nx % 4 == 0; rows per warp in {2,4,8,16,32}
 bool strip_supported(const DevGeo& g, int profile);
 void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& s, void* stream);
-void launch_adj_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& s, void* stream);
+// variant: 0 default registers, unroll 2; 1 <= 64 registers, unroll 1; 2 default, unroll 1;
+// 3 <= 80 registers, unroll 2
+void launch_adj_strip(int rows, int variant, const DevGeo& g, const float* coef, const AdjStep& s, void* stream);
+// two adjoint steps per launch: a = the step producing z(kz), b = the following
+// step producing z(kz-1) (z slots must be four distinct slices)
+void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& a, const AdjStep& b,
+                       void* stream);
 void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, void* stream);
 
 }  // namespace tomo

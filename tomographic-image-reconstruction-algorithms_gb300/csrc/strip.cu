@@ -38,6 +38,23 @@ __device__ __forceinline__ float sponge(int i, int j, int nx, int ny, int w, flo
     return 1.f - smax * x * x;
 }
 
+// Adjoint arithmetic with explicit rounding: the one-step and two-step kernels
+// evaluate every cell with these, so their results agree bit for bit whatever
+// the compiler would otherwise contract into fused multiply-adds.
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+
+// d * ((2 z - z2) + (((ce + cw) + cs) + cn - 4 c z) + inj), products passed in rounded
+__device__ __forceinline__ float adj_cell(float ce, float cw, float cs, float cn, float c, float z, float z2,
+                                          float inj, float d) {
+    const float lz = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(ce, cw), cs), cn), mul(mul(4.f, c), z));
+    return mul(d, __fadd_rn(__fadd_rn(__fsub_rn(mul(2.f, z), z2), lz), inj));
+}
+
+// ((e + w) + s) + n - 4 u
+__device__ __forceinline__ float lap5(float e, float w, float s, float n, float u) {
+    return __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(e, w), s), n), mul(4.f, u));
+}
+
 // West neighbour of element 0 and east neighbour of element 3 of each lane.
 __device__ __forceinline__ void we(const float4& v, const float* __restrict__ row, int lane, int x0, int nx,
                                    float& west, float& east) {
@@ -121,8 +138,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_fwd_strip(DevGeo g, const float*
 }
 
 // ---------------------------------------------------------------------------
-template <int R>
-__global__ void __launch_bounds__(WARPS * 32) k_adj_strip(DevGeo g, const float* __restrict__ coef, AdjStep s) {
+// MINB: minimum resident blocks per SM requested from the register allocator
+// (8 caps registers at 64 per thread); UNR: unroll factor of the row loop.
+template <int R, int MINB, int UNR>
+__global__ void __launch_bounds__(WARPS * 32, MINB) k_adj_strip(DevGeo g, const float* __restrict__ coef,
+                                                               AdjStep s) {
     const int nx = g.nx, ny = g.ny;
     const int gl = blockIdx.z;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -145,7 +165,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_adj_strip(DevGeo g, const float*
     float4 c0 = ld4(coef, (int64_t)y0 * nx + i, act);
     float4 um = ld4(u, (int64_t)(y0 - 1) * nx + i, act && y0 > 0);
     float4 u0 = ld4(u, (int64_t)y0 * nx + i, act);
-#pragma unroll 2
+#pragma unroll UNR
     for (int r = 0; r < R; ++r) {
         const int j = y0 + r;
         if (j >= ny) break;
@@ -156,13 +176,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_adj_strip(DevGeo g, const float*
         const float4 uq = ld4(u, row + nx + i, has_next);
         const float4 zz = ld4(z2, row + i, act);
         // coefficient-weighted neighbours of z(k+1): c*z at west/east via shuffles
-        const float4 cz0 = make_float4(c0.x * z0.x, c0.y * z0.y, c0.z * z0.z, c0.w * z0.w);
+        const float4 cz0 = make_float4(mul(c0.x, z0.x), mul(c0.y, z0.y), mul(c0.z, z0.z), mul(c0.w, z0.w));
         float czw = __shfl_up_sync(FULL, cz0.w, 1), cze = __shfl_down_sync(FULL, cz0.x, 1);
-        if (lane == 0) czw = x0 > 0 ? coef[row + x0 - 1] * z1[row + x0 - 1] : 0.f;
-        if (lane == 31) cze = x0 + STRIP < nx ? coef[row + x0 + STRIP] * z1[row + x0 + STRIP] : 0.f;
+        if (lane == 0) czw = x0 > 0 ? mul(coef[row + x0 - 1], z1[row + x0 - 1]) : 0.f;
+        if (lane == 31) cze = x0 + STRIP < nx ? mul(coef[row + x0 + STRIP], z1[row + x0 + STRIP]) : 0.f;
         float v[4];
-        const float czs[4] = {cm.x * zm.x, cm.y * zm.y, cm.z * zm.z, cm.w * zm.w};
-        const float czn[4] = {cp.x * zp.x, cp.y * zp.y, cp.z * zp.z, cp.w * zp.w};
+        const float czs[4] = {mul(cm.x, zm.x), mul(cm.y, zm.y), mul(cm.z, zm.z), mul(cm.w, zm.w)};
+        const float czn[4] = {mul(cp.x, zp.x), mul(cp.y, zp.y), mul(cp.z, zp.z), mul(cp.w, zp.w)};
         const float cze4[4] = {cz0.y, cz0.z, cz0.w, cze};
         const float czw4[4] = {czw, cz0.x, cz0.y, cz0.z};
         const float zc[4] = {z0.x, z0.y, z0.z, z0.w};
@@ -173,11 +193,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_adj_strip(DevGeo g, const float*
         const int rids[4] = {rid.x, rid.y, rid.z, rid.w};
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
-            const float lz = (((cze4[t] + czw4[t]) + czs[t]) + czn[t]) - 4.f * cc[t] * zc[t];
             const float inj = rids[t] >= 0 ? rr[rids[t]] : 0.f;
             float d = 1.f;
             if (edge_x || near_y) d = sponge(i + t, j, nx, ny, g.sponge_w, g.sponge_max);
-            v[t] = d * ((2.f * zc[t] - z2v[t]) + lz + inj);
+            v[t] = adj_cell(cze4[t], czw4[t], czs[t], czn[t], cc[t], zc[t], z2v[t], inj, d);
         }
         // Laplacian of the forward slice (zero outside the grid)
         float uw, ue;
@@ -191,11 +210,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_adj_strip(DevGeo g, const float*
             float4 cr = *reinterpret_cast<const float4*>(corr + row + i);
             float lu[4];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) lu[t] = (((uue[t] + uuw[t]) + uus[t]) + uun[t]) - 4.f * uc4[t];
-            cr.x += v[0] * lu[0];
-            cr.y += v[1] * lu[1];
-            cr.z += v[2] * lu[2];
-            cr.w += v[3] * lu[3];
+            for (int t = 0; t < 4; ++t) lu[t] = lap5(uue[t], uuw[t], uus[t], uun[t], uc4[t]);
+            cr.x = __fmaf_rn(v[0], lu[0], cr.x);
+            cr.y = __fmaf_rn(v[1], lu[1], cr.y);
+            cr.z = __fmaf_rn(v[2], lu[2], cr.z);
+            cr.w = __fmaf_rn(v[3], lu[3], cr.w);
             *reinterpret_cast<float4*>(corr + row + i) = cr;
             *reinterpret_cast<float4*>(zk + row + i) = make_float4(v[0], v[1], v[2], v[3]);
         }
@@ -221,6 +240,147 @@ __global__ void __launch_bounds__(256) k_resid_parts(const float* __restrict__ r
     if (threadIdx.x == 0) part[(int64_t)gl * nt + k] = red[0];
 }
 
+// ---------------------------------------------------------------------------
+// Two adjoint steps per launch (temporal blocking in registers).  A lane holds
+// two cells; strips are 64 cells wide and overlap by one lane (2 cells) on each
+// side, so lanes 0 and 31 compute the first step as halo for their neighbours
+// and only lanes 1..30 (60 cells) write.  Rows y0-1 .. y0+R of the first step
+// z(kz) roll through registers and the second step z(kz-1) is computed one row
+// behind.  Both slices, and the correlation with u(q) and u(q-1), are written
+// once per launch: per cell-update this moves z(kz+1), z(kz+2), u(q), u(q-1),
+// the coefficient and the correlation once per two steps.  The z ring has four
+// slots, so the second step never overwrites a slice another warp still reads.
+// Both kernels evaluate cells with adj_cell/lap5 and fused correlation updates,
+// so the results are identical to two one-step launches.
+struct Adj2Step {
+    const float* z2;    // z(kz+2)
+    const float* z1;    // z(kz+1)
+    float* za;          // z(kz)   out
+    float* zb;          // z(kz-1) out
+    int64_t zstride;
+    const float* ua;    // u(q)   correlated with z(kz)
+    const float* ub;    // u(q-1) correlated with z(kz-1)
+    int64_t ustride;
+    const float* rra;   // residual of pass-group 0 at step kz
+    const float* rrb;   // at step kz-1
+    int64_t rrstride;
+    float* corr;
+    int64_t cstride;
+    int ng;
+};
+
+__device__ __forceinline__ float2 ld2(const float* __restrict__ p, int64_t off, bool ok) {
+    return ok ? *reinterpret_cast<const float2*>(p + off) : make_float2(0.f, 0.f);
+}
+
+template <int R>
+__global__ void __launch_bounds__(WARPS * 32, 8) k_adj2_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 60 - 2;
+    const int i = x0 + 2 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    const bool in = i >= 0 && i < nx;
+    const bool own = in && lane >= 1 && lane <= 30;
+    const float* z1 = s.z1 + gl * s.zstride;
+    const float* z2 = s.z2 + gl * s.zstride;
+    float* za = s.za + gl * s.zstride;
+    float* zb = s.zb + gl * s.zstride;
+    const float* ua = s.ua + gl * s.ustride;
+    const float* ub = s.ub + gl * s.ustride;
+    const float* rra = s.rra + gl * s.rrstride;
+    const float* rrb = s.rrb + gl * s.rrstride;
+    float* corr = s.corr + gl * s.cstride;
+    const bool edge_x = x0 < g.sponge_w || x0 + 64 > nx - g.sponge_w;
+    auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
+    // rolling state at the top of iteration r
+    float2 z1m = ld2(z1, (int64_t)(y0 - 2) * nx + i, row_ok(y0 - 2));
+    float2 z10 = ld2(z1, (int64_t)(y0 - 1) * nx + i, row_ok(y0 - 1));
+    float2 cm2 = make_float2(0.f, 0.f);
+    float2 cm = ld2(coef, (int64_t)(y0 - 2) * nx + i, row_ok(y0 - 2));
+    float2 c0 = ld2(coef, (int64_t)(y0 - 1) * nx + i, row_ok(y0 - 1));
+    float2 zam2 = make_float2(0.f, 0.f), zam = make_float2(0.f, 0.f);
+    float2 uam2 = make_float2(0.f, 0.f), uam = make_float2(0.f, 0.f);
+    float2 ubm2 = make_float2(0.f, 0.f), ubm = make_float2(0.f, 0.f);
+    int2 ridm = make_int2(-1, -1);
+#pragma unroll 1
+    for (int r = y0 - 1; r <= y0 + R; ++r) {
+        if (r > ny) break;
+        const int64_t row = (int64_t)r * nx;
+        const bool ok = row_ok(r);
+        const float2 z1p = ld2(z1, row + nx + i, row_ok(r + 1));
+        const float2 cp = ld2(coef, row + nx + i, row_ok(r + 1));
+        const float2 zz = ld2(z2, row + i, ok);
+        const float2 ua0 = ld2(ua, row + i, ok);
+        const float2 ub0 = ld2(ub, row + i, ok);
+        const int2 rid = ok ? *reinterpret_cast<const int2*>(g.rid + row + i) : make_int2(-1, -1);
+        // ---- first step: z(kz) at row r (all lanes; zero outside the grid)
+        float2 za0 = make_float2(0.f, 0.f);
+        {
+            const float cz0x = mul(c0.x, z10.x), cz0y = mul(c0.y, z10.y);
+            float czw = __shfl_up_sync(FULL, cz0y, 1), cze = __shfl_down_sync(FULL, cz0x, 1);
+            if (lane == 0) czw = (ok && x0 > 0) ? mul(coef[row + x0 - 1], z1[row + x0 - 1]) : 0.f;
+            if (lane == 31) cze = (ok && x0 + 64 < nx) ? mul(coef[row + x0 + 64], z1[row + x0 + 64]) : 0.f;
+            if (ok) {
+                const bool near = edge_x || r < g.sponge_w || r >= ny - g.sponge_w;
+                const float ix = rid.x >= 0 ? rra[rid.x] : 0.f;
+                const float iy = rid.y >= 0 ? rra[rid.y] : 0.f;
+                const float dx = near ? sponge(i, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+                const float dy = near ? sponge(i + 1, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+                za0.x = adj_cell(cz0y, czw, mul(cm.x, z1m.x), mul(cp.x, z1p.x), c0.x, z10.x, zz.x, ix, dx);
+                za0.y = adj_cell(cze, cz0x, mul(cm.y, z1m.y), mul(cp.y, z1p.y), c0.y, z10.y, zz.y, iy, dy);
+            }
+        }
+        // ---- second step: z(kz-1) at row r-1, correlation of both steps at row r-1
+        const int rb = r - 1;
+        {
+            // every lane joins the shuffles
+            const float czax = mul(cm.x, zam.x), czay = mul(cm.y, zam.y);
+            const float czw = __shfl_up_sync(FULL, czay, 1), cze = __shfl_down_sync(FULL, czax, 1);
+            const float uaw = __shfl_up_sync(FULL, uam.y, 1), uae = __shfl_down_sync(FULL, uam.x, 1);
+            const float ubw = __shfl_up_sync(FULL, ubm.y, 1), ube = __shfl_down_sync(FULL, ubm.x, 1);
+            if (own && rb >= y0 && rb < ny) {
+                const bool near = edge_x || rb < g.sponge_w || rb >= ny - g.sponge_w;
+                const int64_t rowb = (int64_t)rb * nx;
+                const float ix = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
+                const float iy = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
+                const float dx = near ? sponge(i, rb, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+                const float dy = near ? sponge(i + 1, rb, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+                float2 zbv;
+                zbv.x = adj_cell(czay, czw, mul(cm2.x, zam2.x), mul(c0.x, za0.x), cm.x, zam.x, z1m.x, ix, dx);
+                zbv.y = adj_cell(cze, czax, mul(cm2.y, zam2.y), mul(c0.y, za0.y), cm.y, zam.y, z1m.y, iy, dy);
+                const float lax = lap5(uam.y, uaw, uam2.x, ua0.x, uam.x);
+                const float lay = lap5(uae, uam.x, uam2.y, ua0.y, uam.y);
+                const float lbx = lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x);
+                const float lby = lap5(ube, ubm.x, ubm2.y, ub0.y, ubm.y);
+                float2 cr = *reinterpret_cast<const float2*>(corr + rowb + i);
+                cr.x = __fmaf_rn(zam.x, lax, cr.x);
+                cr.y = __fmaf_rn(zam.y, lay, cr.y);
+                cr.x = __fmaf_rn(zbv.x, lbx, cr.x);
+                cr.y = __fmaf_rn(zbv.y, lby, cr.y);
+                *reinterpret_cast<float2*>(corr + rowb + i) = cr;
+                *reinterpret_cast<float2*>(za + rowb + i) = zam;
+                *reinterpret_cast<float2*>(zb + rowb + i) = zbv;
+            }
+        }
+        z1m = z10; z10 = z1p;
+        cm2 = cm; cm = c0; c0 = cp;
+        zam2 = zam; zam = za0;
+        uam2 = uam; uam = ua0;
+        ubm2 = ubm; ubm = ub0;
+        ridm = rid;
+    }
+}
+
+template <int R>
+void adj2_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    dim3 grid((g.nx + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
+    k_adj2_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+}
+
 template <int R>
 void fwd_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
@@ -229,10 +389,15 @@ void fwd_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_
 }
 
 template <int R>
-void adj_strip(const DevGeo& g, const float* coef, const AdjStep& s, cudaStream_t st) {
+void adj_strip(int variant, const DevGeo& g, const float* coef, const AdjStep& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     dim3 grid((g.nx + STRIP - 1) / STRIP, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
-    k_adj_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+    switch (variant) {
+    case 1: k_adj_strip<R, 8, 1><<<grid, WARPS * 32, 0, st>>>(g, coef, s); break;
+    case 2: k_adj_strip<R, 1, 1><<<grid, WARPS * 32, 0, st>>>(g, coef, s); break;
+    case 3: k_adj_strip<R, 6, 2><<<grid, WARPS * 32, 0, st>>>(g, coef, s); break;
+    default: k_adj_strip<R, 1, 2><<<grid, WARPS * 32, 0, st>>>(g, coef, s); break;
+    }
 }
 
 }  // namespace
@@ -242,6 +407,22 @@ void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, 
 }
 
 bool strip_supported(const DevGeo& g, int profile) { return profile == TOMO_PROFILE_CFG && g.nx % 4 == 0; }
+
+void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& a, const AdjStep& b,
+                       void* stream) {
+    Adj2Step s{};
+    s.z2 = a.z2; s.z1 = a.z1; s.za = a.zk; s.zb = b.zk; s.zstride = a.zstride;
+    s.ua = a.uq; s.ub = b.uq; s.ustride = a.ustride;
+    s.rra = a.rr; s.rrb = b.rr; s.rrstride = a.rrstride;
+    s.corr = a.corr; s.cstride = a.cstride; s.ng = a.ng;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (rows) {
+    case 4: adj2_strip<4>(g, coef, s, st); break;
+    case 16: adj2_strip<16>(g, coef, s, st); break;
+    case 32: adj2_strip<32>(g, coef, s, st); break;
+    default: adj2_strip<8>(g, coef, s, st); break;
+    }
+}
 
 void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& s, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
@@ -254,14 +435,14 @@ void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdSte
     }
 }
 
-void launch_adj_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& s, void* stream) {
+void launch_adj_strip(int rows, int variant, const DevGeo& g, const float* coef, const AdjStep& s, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     switch (rows) {
-    case 2: adj_strip<2>(g, coef, s, st); break;
-    case 4: adj_strip<4>(g, coef, s, st); break;
-    case 16: adj_strip<16>(g, coef, s, st); break;
-    case 32: adj_strip<32>(g, coef, s, st); break;
-    default: adj_strip<8>(g, coef, s, st); break;
+    case 2: adj_strip<2>(variant, g, coef, s, st); break;
+    case 4: adj_strip<4>(variant, g, coef, s, st); break;
+    case 16: adj_strip<16>(variant, g, coef, s, st); break;
+    case 32: adj_strip<32>(variant, g, coef, s, st); break;
+    default: adj_strip<8>(variant, g, coef, s, st); break;
     }
 }
 
