@@ -235,3 +235,28 @@ def test_errors_are_status_codes():
         with pytest.raises(tomo.TomoError) as e:
             ctx.iterate(99, tomo.schedule(omega=1.0), 0, f, np.zeros(ctx.records_shape(), np.float32))
         assert e.value.status == tomo.ERR_ARG
+
+
+@pytest.mark.parametrize("nt", [180, 181])
+def test_two_step_kernels_match_one_step(nt, monkeypatch):
+    """Two time steps per launch (forward and adjoint) give the same bits as one."""
+    fo = blob_phantom(64, 72, seed=8)
+    cfg0 = small_cfg(nt=nt, ckpt_interval=9)
+    meas = O.forward(cfg0, fo.astype(np.float64))
+    f0 = blob_phantom(64, 72, seed=9, amp=0.01)
+    outs = []
+    for pair, fwd_rows in (("0", "4"), ("1", "4"), ("1", "104")):   # 104: four cells per lane
+        monkeypatch.setenv("TOMO_STRIP_ROWS", "4")
+        monkeypatch.setenv("TOMO_FWD_PAIR", pair)
+        monkeypatch.setenv("TOMO_FWD_PAIR_ROWS", fwd_rows)
+        monkeypatch.setenv("TOMO_ADJ_PAIR", pair)
+        with tomo.Context(small_cfg(nt=nt, ckpt_interval=9)) as ctx:
+            rec = ctx.forward(fo)
+            dfg, _, r2 = ctx.gradient(f0, meas)
+        outs.append((rec, dfg, r2))
+    for o in outs[1:]:
+        assert np.array_equal(outs[0][0], o[0])
+        assert np.array_equal(outs[0][1], o[1])
+        assert outs[0][2] == o[2]
+    rec_o = O.forward(cfg0, fo.astype(np.float64))
+    assert rel(outs[1][0], rec_o) <= TOL_FIELD

@@ -68,6 +68,8 @@ struct tomo_ctx {
     int rows_fwd = 8, rows_adj = 8, adj_variant = 0;
     bool adj_pair = false;       // two adjoint steps per launch (strip kernels)
     int rows_adj2 = 8;
+    bool fwd_pair = false;       // two forward steps per launch (needs S >= 4)
+    int rows_fwd2 = 8;
     static constexpr int ZR = 4; // adjoint ring slots
     bool tuned = false;
     std::vector<void*> allocs;
@@ -179,6 +181,9 @@ tomo_status autotune(tomo_ctx* c) {
         c->rows_fwd = c->rows_adj = c->rows_adj2 = std::atoi(e);
         if (const char* v = std::getenv("TOMO_ADJ_VARIANT")) c->adj_variant = std::atoi(v);
         if (const char* v = std::getenv("TOMO_ADJ_PAIR")) c->adj_pair = std::atoi(v) != 0;
+        if (const char* v = std::getenv("TOMO_FWD_PAIR")) c->fwd_pair = std::atoi(v) != 0 && c->S >= 4;
+        c->rows_fwd2 = c->rows_fwd;
+        if (const char* v = std::getenv("TOMO_FWD_PAIR_ROWS")) c->rows_fwd2 = std::atoi(v);
         return TOMO_OK;
     }
     const int cands[5] = {2, 4, 8, 16, 32};
@@ -202,6 +207,20 @@ tomo_status autotune(tomo_ctx* c) {
             }
             if (which == 0 && ms < best_f) { best_f = ms; c->rows_fwd = rows; }
             if (which > 0 && ms < best_a) { best_a = ms; c->rows_adj = rows; c->adj_variant = which - 1; }
+        }
+        for (int code : {rows, 100 + rows}) {   // two forward steps per launch, 2 or 4 cells per lane
+            if (rows < 4 || c->S < 4) break;
+            float ms = 0.f;
+            for (int pass = 0; pass < 2; ++pass) {
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                for (int t = 0; t < reps; t += 2)
+                    launch_fwd2_strip(code, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), fwd_args(c, k0 + t + 1, 0, ng),
+                                      false, false, c->st);
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            }
+            if (ms < best_f) { best_f = ms; c->rows_fwd2 = code; c->fwd_pair = true; }
         }
         if (rows >= 4) {   // two steps per launch: reps/2 launches cover the same steps
             float ms = 0.f;
@@ -334,25 +353,42 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     ++n;
     const float* meas_g = c->meas + (int64_t)g0 * rpg;
     float* out_g = mode == MODE_GRAD ? c->rr : c->rec + (int64_t)g0 * rpg;
-    for (int k = 1; k <= nt - 2; ++k) {
+    // checkpoint copy of slice m: chunk ch >= 1 starts at qa = 1 + ch*K and keeps slices qa-1 and qa
+    auto ck_of = [&](FwdStep& fs, int m) {
+        if (mode != MODE_GRAD || c->full) return;
+        int ch = -1, which = 0;
+        if (m % K == 0) { ch = m / K; which = 0; }
+        else if ((m - 1) % K == 0) { ch = (m - 1) / K; which = 1; }
+        if (ch >= 1 && ch < c->nchunk) {
+            fs.ck = c->ckpt + ((int64_t)ch * 2 + which) * N;
+            fs.ckstride = (int64_t)c->nchunk * 2 * N;
+        }
+    };
+    int gnext = 2;   // strip path: slices 2 .. gnext-1 are recorded, in order
+    for (int k = 1; k <= nt - 2;) {
         FwdStep fs = fwd_args(c, k, g0, ng);
         const int m = k + 1;
-        if (mode == MODE_GRAD && !c->full) {
-            // chunk ch >= 1 starts at qa = 1 + ch*K and keeps slices qa-1 and qa.
-            int ch = -1, which = 0;
-            if (m % K == 0) { ch = m / K; which = 0; }
-            else if ((m - 1) % K == 0) { ch = (m - 1) / K; which = 1; }
-            if (ch >= 1 && ch < c->nchunk) {
-                fs.ck = c->ckpt + ((int64_t)ch * 2 + which) * N;
-                fs.ckstride = (int64_t)c->nchunk * 2 * N;
-            }
-        }
+        ck_of(fs, m);
         if (c->strip) {
-            // slice k is gathered by the launch that computes slice k+1
-            fs.gk = k;
             fs.gmeas = mode == MODE_GRAD ? meas_g : nullptr;
             fs.gout = out_g;
-            fwd_launch(c, fs);
+            if (c->fwd_pair && k + 1 <= nt - 2) {
+                // slices k+1 and k+2; records slices k-1 and k from the launch's inputs
+                FwdStep fb = fwd_args(c, k + 1, g0, ng);
+                ck_of(fb, m + 1);
+                const bool gp = (k - 1 == gnext);
+                if (gp) ++gnext;
+                const bool gc = (k == gnext);
+                if (gc) ++gnext;
+                launch_fwd2_strip(c->rows_fwd2, c->dg, c->coef, fs, fb, gp, gc, st);
+                k += 2;
+            } else {
+                // slice k is gathered by the launch that computes slice k+1
+                fs.gk = (k == gnext) ? k : -1;
+                if (k == gnext) ++gnext;
+                fwd_launch(c, fs);
+                k += 1;
+            }
             ++n;
             continue;
         }
@@ -367,6 +403,20 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         gs.part = mode == MODE_GRAD ? c->rpart + (int64_t)g0 * nt : nullptr;
         launch_gather(c->dg, gs, st);
         n += 2;
+        k += 1;
+    }
+    if (c->strip) {
+        for (int m = std::max(gnext, 2); m < nt - 1; ++m) {   // slices left before the last
+            GatherStep gs{};
+            gs.u = c->hist + c->slot(m);
+            gs.gstride = gstride;
+            gs.k = m;
+            gs.ng = ng;
+            gs.meas = mode == MODE_GRAD ? meas_g : nullptr;
+            gs.out = out_g;
+            launch_gather(c->dg, gs, st);
+            ++n;
+        }
     }
     if (c->strip) {
         GatherStep gs{};
@@ -403,8 +453,15 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
                     launch_copy_groups(c->hist + c->slot(qa), gstride, c->ckpt + ((int64_t)ch * 2 + 1) * N, cks, ng,
                                        N, st);
                 }
-                for (int m = qa + 1; m <= qb; ++m) {
-                    fwd_launch(c, fwd_args(c, m - 1, g0, ng));
+                for (int m = qa + 1; m <= qb;) {
+                    if (c->strip && c->fwd_pair && m + 1 <= qb) {
+                        launch_fwd2_strip(c->rows_fwd2, c->dg, c->coef, fwd_args(c, m - 1, g0, ng),
+                                          fwd_args(c, m, g0, ng), false, false, st);
+                        m += 2;
+                    } else {
+                        fwd_launch(c, fwd_args(c, m - 1, g0, ng));
+                        m += 1;
+                    }
                     ++n;
                 }
             }
@@ -870,7 +927,11 @@ tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* 
     TRY(autotune(c));
     CU(c, cudaEventRecord(c->ev0, c->st));
     for (int t = 0; t < steps;) {
-        if (which == 0) {
+        if (which == 0 && c->fwd_pair && t + 1 < steps) {
+            launch_fwd2_strip(c->rows_fwd2, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), fwd_args(c, k0 + t + 1, 0, ng),
+                              false, false, c->st);
+            t += 2;
+        } else if (which == 0) {
             fwd_launch(c, fwd_args(c, k0 + t, 0, ng));
             t += 1;
         } else if (c->adj_pair && t + 1 < steps) {

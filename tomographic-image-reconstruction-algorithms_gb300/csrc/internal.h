@@ -157,6 +157,11 @@ void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdSte
 // variant: 0 default registers, unroll 2; 1 <= 64 registers, unroll 1; 2 default, unroll 1;
 // 3 <= 80 registers, unroll 2
 void launch_adj_strip(int rows, int variant, const DevGeo& g, const float* coef, const AdjStep& s, void* stream);
+// two forward steps per launch: a computes slice k+1, b slice k+2 (a.un, b.un; four
+// distinct slots); gather_prev / gather_cur record slices k-1 / k into a.gout.
+// rows in {4,8,16,32}: two cells per lane; 100 + rows: four cells per lane
+void launch_fwd2_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& a, const FwdStep& b,
+                       bool gather_prev, bool gather_cur, void* stream);
 // two adjoint steps per launch: a = the step producing z(kz), b = the following
 // step producing z(kz-1) (z slots must be four distinct slices)
 void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& a, const AdjStep& b,

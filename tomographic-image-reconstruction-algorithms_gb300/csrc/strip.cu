@@ -55,6 +55,22 @@ __device__ __forceinline__ float lap5(float e, float w, float s, float n, float 
     return __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(e, w), s), n), mul(4.f, u));
 }
 
+// Forward cell update d * ((2 u - up) + c * lap) + a, explicit rounding (shared by
+// the one-step and two-step forward kernels).
+__device__ __forceinline__ float fwd_cell(float e, float w, float s, float n, float u, float up, float c, float d,
+                                          float a) {
+    const float v = __fadd_rn(__fsub_rn(mul(2.f, u), up), mul(c, lap5(e, w, s, n, u)));
+    return __fadd_rn(mul(d, v), a);
+}
+
+// Source amplitude a at cell q of group g at step k (0 when q emits nothing).
+__device__ __forceinline__ float emit_at(const int32_t* em, int gs, int64_t q, float a) {
+    float r = 0.f;
+    for (int t = 0; t < gs; ++t)
+        if (em[t] == q) r += a;
+    return r;
+}
+
 // West neighbour of element 0 and east neighbour of element 3 of each lane.
 __device__ __forceinline__ void we(const float4& v, const float* __restrict__ row, int lane, int x0, int nx,
                                    float& west, float& east) {
@@ -107,27 +123,21 @@ __global__ void __launch_bounds__(WARPS * 32) k_fwd_strip(DevGeo g, const float*
         const float4 c = ld4(coef, row + i, act);
         float w, e;
         we(r0, uc + row, lane, x0, nx, w, e);
+        const bool near = edge_x || j < g.sponge_w || j >= ny - g.sponge_w;
+        const float dx = near ? sponge(i, j, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+        const float dy = near ? sponge(i + 1, j, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+        const float dz = near ? sponge(i + 2, j, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+        const float dw = near ? sponge(i + 3, j, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+        const int64_t q0 = row + i;
+        const float ax = src ? emit_at(em, g.gs, q0, a) : 0.f;
+        const float ay = src ? emit_at(em, g.gs, q0 + 1, a) : 0.f;
+        const float az = src ? emit_at(em, g.gs, q0 + 2, a) : 0.f;
+        const float aw = src ? emit_at(em, g.gs, q0 + 3, a) : 0.f;
         float4 v;
-        v.x = (2.f * r0.x - p.x) + c.x * ((((r0.y + w) + rm.x) + rp.x) - 4.f * r0.x);
-        v.y = (2.f * r0.y - p.y) + c.y * ((((r0.z + r0.x) + rm.y) + rp.y) - 4.f * r0.y);
-        v.z = (2.f * r0.z - p.z) + c.z * ((((r0.w + r0.y) + rm.z) + rp.z) - 4.f * r0.z);
-        v.w = (2.f * r0.w - p.w) + c.w * ((((e + r0.z) + rm.w) + rp.w) - 4.f * r0.w);
-        if (edge_x || j < g.sponge_w || j >= ny - g.sponge_w) {
-            v.x *= sponge(i, j, nx, ny, g.sponge_w, g.sponge_max);
-            v.y *= sponge(i + 1, j, nx, ny, g.sponge_w, g.sponge_max);
-            v.z *= sponge(i + 2, j, nx, ny, g.sponge_w, g.sponge_max);
-            v.w *= sponge(i + 3, j, nx, ny, g.sponge_w, g.sponge_max);
-        }
-        if (src) {
-            const int64_t q0 = row + i;
-            for (int t = 0; t < g.gs; ++t) {
-                const int64_t d = (int64_t)em[t] - q0;
-                if (d == 0) v.x += a;
-                else if (d == 1) v.y += a;
-                else if (d == 2) v.z += a;
-                else if (d == 3) v.w += a;
-            }
-        }
+        v.x = fwd_cell(r0.y, w, rm.x, rp.x, r0.x, p.x, c.x, dx, ax);
+        v.y = fwd_cell(r0.z, r0.x, rm.y, rp.y, r0.y, p.y, c.y, dy, ay);
+        v.z = fwd_cell(r0.w, r0.y, rm.z, rp.z, r0.z, p.z, c.z, dz, az);
+        v.w = fwd_cell(e, r0.z, rm.w, rp.w, r0.w, p.w, c.w, dw, aw);
         if (act) {
             *reinterpret_cast<float4*>(un + row + i) = v;
             if (ck) *reinterpret_cast<float4*>(ck + row + i) = v;
@@ -381,6 +391,219 @@ void adj2_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStrea
     k_adj2_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
 }
 
+// ---------------------------------------------------------------------------
+// Two forward steps per launch.  Same strip geometry as k_adj2_strip (2 cells
+// per lane, 64-cell strips overlapping by one lane each side, lanes 1..30
+// write).  u(k+1) rows y0-1 .. y0+R roll through registers and u(k+2) follows
+// one row behind, so u(k-1), u(k) and the coefficient are read once per two
+// steps; both new slices are written (the next launch and the adjoint need
+// them).  The gather blocks record the two input slices, which are complete.
+struct Fwd2Step {
+    const float* up;   // u(k-1)
+    const float* uc;   // u(k)
+    float* u1;         // u(k+1) out
+    float* u2;         // u(k+2) out
+    int64_t gstride;
+    float* ck1;        // optional checkpoint copies of u(k+1), u(k+2) (pass-group 0)
+    float* ck2;
+    int64_t ckstride;
+    int k, g0, ng;
+    int gka, gkb;      // slices gathered from up (k-1) and uc (k); < 2: none
+    const float* gmeas;
+    float* gout;
+};
+
+__device__ __forceinline__ void gather_slice(const DevGeo& g, const float* u, int gl, int gk, const float* gmeas,
+                                             float* gout) {
+    const int64_t base = ((int64_t)gl * g.nt + gk) * g.nch;
+    for (int c = threadIdx.x; c < g.nch; c += blockDim.x) {
+        const int cell = g.rcv[c];
+        const float v = cell >= 0 ? u[cell] : 0.f;
+        gout[base + c] = gmeas ? (cell >= 0 ? gmeas[base + c] - v : 0.f) : v;
+    }
+}
+
+template <int R>
+__global__ void __launch_bounds__(WARPS * 32, 8) k_fwd2_strip(DevGeo g, const float* __restrict__ coef, Fwd2Step s) {
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    if (blockIdx.y == gridDim.y - 1) {
+        if (blockIdx.x != 0) return;
+        if (s.gka >= 2) gather_slice(g, s.up + gl * s.gstride, gl, s.gka, s.gmeas, s.gout);
+        if (s.gkb >= 2) gather_slice(g, s.uc + gl * s.gstride, gl, s.gkb, s.gmeas, s.gout);
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 60 - 2;
+    const int i = x0 + 2 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    const bool in = i >= 0 && i < nx;
+    const bool own = in && lane >= 1 && lane <= 30;
+    const float* uc = s.uc + gl * s.gstride;
+    const float* up = s.up + gl * s.gstride;
+    float* u1 = s.u1 + gl * s.gstride;
+    float* u2 = s.u2 + gl * s.gstride;
+    float* ck1 = s.ck1 ? s.ck1 + gl * s.ckstride : nullptr;
+    float* ck2 = s.ck2 ? s.ck2 + gl * s.ckstride : nullptr;
+    const bool edge_x = x0 < g.sponge_w || x0 + 64 > nx - g.sponge_w;
+    const int32_t* em = g.emit + (int64_t)(s.g0 + gl) * g.gs;
+    const bool src1 = s.k < g.n_src_steps, src2 = s.k + 1 < g.n_src_steps;
+    const float a1 = src1 ? g.src[s.k] : 0.f, a2 = src2 ? g.src[s.k + 1] : 0.f;
+    auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
+    float2 u0m = ld2(uc, (int64_t)(y0 - 2) * nx + i, row_ok(y0 - 2));
+    float2 u00 = ld2(uc, (int64_t)(y0 - 1) * nx + i, row_ok(y0 - 1));
+    float2 cm = ld2(coef, (int64_t)(y0 - 2) * nx + i, row_ok(y0 - 2));
+    float2 v1m2 = make_float2(0.f, 0.f), v1m = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int r = y0 - 1; r <= y0 + R; ++r) {
+        if (r > ny) break;
+        const int64_t row = (int64_t)r * nx;
+        const bool ok = row_ok(r);
+        const float2 u0p = ld2(uc, row + nx + i, row_ok(r + 1));
+        const float2 p = ld2(up, row + i, ok);
+        const float2 c0 = ld2(coef, row + i, ok);
+        // ---- u(k+1) at row r, all lanes (zero outside the grid)
+        float w = __shfl_up_sync(FULL, u00.y, 1), e = __shfl_down_sync(FULL, u00.x, 1);
+        if (lane == 0) w = (ok && x0 > 0) ? uc[row + x0 - 1] : 0.f;
+        if (lane == 31) e = (ok && x0 + 64 < nx) ? uc[row + x0 + 64] : 0.f;
+        float2 v10 = make_float2(0.f, 0.f);
+        if (ok) {
+            const bool near = edge_x || r < g.sponge_w || r >= ny - g.sponge_w;
+            const float dx = near ? sponge(i, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+            const float dy = near ? sponge(i + 1, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+            const float ax = src1 ? emit_at(em, g.gs, row + i, a1) : 0.f;
+            const float ay = src1 ? emit_at(em, g.gs, row + i + 1, a1) : 0.f;
+            v10.x = fwd_cell(u00.y, w, u0m.x, u0p.x, u00.x, p.x, c0.x, dx, ax);
+            v10.y = fwd_cell(e, u00.x, u0m.y, u0p.y, u00.y, p.y, c0.y, dy, ay);
+        }
+        // ---- u(k+2) at row r-1
+        const int rb = r - 1;
+        const float w2 = __shfl_up_sync(FULL, v1m.y, 1), e2 = __shfl_down_sync(FULL, v1m.x, 1);
+        if (own && rb >= y0 && rb < ny) {
+            const int64_t rowb = (int64_t)rb * nx;
+            const bool near = edge_x || rb < g.sponge_w || rb >= ny - g.sponge_w;
+            const float dx = near ? sponge(i, rb, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+            const float dy = near ? sponge(i + 1, rb, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+            const float ax = src2 ? emit_at(em, g.gs, rowb + i, a2) : 0.f;
+            const float ay = src2 ? emit_at(em, g.gs, rowb + i + 1, a2) : 0.f;
+            float2 v2;
+            v2.x = fwd_cell(v1m.y, w2, v1m2.x, v10.x, v1m.x, u0m.x, cm.x, dx, ax);
+            v2.y = fwd_cell(e2, v1m.x, v1m2.y, v10.y, v1m.y, u0m.y, cm.y, dy, ay);
+            *reinterpret_cast<float2*>(u1 + rowb + i) = v1m;
+            *reinterpret_cast<float2*>(u2 + rowb + i) = v2;
+            if (ck1) *reinterpret_cast<float2*>(ck1 + rowb + i) = v1m;
+            if (ck2) *reinterpret_cast<float2*>(ck2 + rowb + i) = v2;
+        }
+        u0m = u00; u00 = u0p;
+        cm = c0;
+        v1m2 = v1m; v1m = v10;
+    }
+}
+
+// Same two-step forward with four cells per lane: 128-cell strips overlapping
+// by one lane (4 cells) on each side, lanes 1..30 (120 cells) write, 16-byte
+// accesses.
+__device__ __forceinline__ float4 fwd_row4(const float4& u, float w, float e, const float4& s, const float4& n,
+                                           const float4& up, const float4& c, const float d[4], const float a[4]) {
+    float4 v;
+    v.x = fwd_cell(u.y, w, s.x, n.x, u.x, up.x, c.x, d[0], a[0]);
+    v.y = fwd_cell(u.z, u.x, s.y, n.y, u.y, up.y, c.y, d[1], a[1]);
+    v.z = fwd_cell(u.w, u.y, s.z, n.z, u.z, up.z, c.z, d[2], a[2]);
+    v.w = fwd_cell(e, u.z, s.w, n.w, u.w, up.w, c.w, d[3], a[3]);
+    return v;
+}
+
+template <int R>
+__global__ void __launch_bounds__(WARPS * 32, 6) k_fwd2q_strip(DevGeo g, const float* __restrict__ coef, Fwd2Step s) {
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    if (blockIdx.y == gridDim.y - 1) {
+        if (blockIdx.x != 0) return;
+        if (s.gka >= 2) gather_slice(g, s.up + gl * s.gstride, gl, s.gka, s.gmeas, s.gout);
+        if (s.gkb >= 2) gather_slice(g, s.uc + gl * s.gstride, gl, s.gkb, s.gmeas, s.gout);
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 120 - 4;
+    const int i = x0 + 4 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    const bool in = i >= 0 && i < nx;
+    const bool own = in && lane >= 1 && lane <= 30;
+    const float* uc = s.uc + gl * s.gstride;
+    const float* up = s.up + gl * s.gstride;
+    float* u1 = s.u1 + gl * s.gstride;
+    float* u2 = s.u2 + gl * s.gstride;
+    float* ck1 = s.ck1 ? s.ck1 + gl * s.ckstride : nullptr;
+    float* ck2 = s.ck2 ? s.ck2 + gl * s.ckstride : nullptr;
+    const bool edge_x = x0 < g.sponge_w || x0 + STRIP > nx - g.sponge_w;
+    const int32_t* em = g.emit + (int64_t)(s.g0 + gl) * g.gs;
+    const bool src1 = s.k < g.n_src_steps, src2 = s.k + 1 < g.n_src_steps;
+    const float a1 = src1 ? g.src[s.k] : 0.f, a2 = src2 ? g.src[s.k + 1] : 0.f;
+    auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
+    auto factors = [&](int r, bool srcf, float amp, float d[4], float a[4]) {
+        const bool near = edge_x || r < g.sponge_w || r >= ny - g.sponge_w;
+        const int64_t q = (int64_t)r * nx + i;
+        for (int t = 0; t < 4; ++t) {
+            d[t] = near ? sponge(i + t, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+            a[t] = srcf ? emit_at(em, g.gs, q + t, amp) : 0.f;
+        }
+    };
+    float4 u0m = ld4(uc, (int64_t)(y0 - 2) * nx + i, row_ok(y0 - 2));
+    float4 u00 = ld4(uc, (int64_t)(y0 - 1) * nx + i, row_ok(y0 - 1));
+    float4 cm = ld4(coef, (int64_t)(y0 - 2) * nx + i, row_ok(y0 - 2));
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 v1m2 = zero4, v1m = zero4;
+#pragma unroll 1
+    for (int r = y0 - 1; r <= y0 + R; ++r) {
+        if (r > ny) break;
+        const int64_t row = (int64_t)r * nx;
+        const bool ok = row_ok(r);
+        const float4 u0p = ld4(uc, row + nx + i, row_ok(r + 1));
+        const float4 p = ld4(up, row + i, ok);
+        const float4 c0 = ld4(coef, row + i, ok);
+        float w = __shfl_up_sync(FULL, u00.w, 1), e = __shfl_down_sync(FULL, u00.x, 1);
+        if (lane == 0) w = (ok && x0 > 0) ? uc[row + x0 - 1] : 0.f;
+        if (lane == 31) e = (ok && x0 + STRIP < nx) ? uc[row + x0 + STRIP] : 0.f;
+        float4 v10 = zero4;
+        if (ok) {
+            float d[4], a[4];
+            factors(r, src1, a1, d, a);
+            v10 = fwd_row4(u00, w, e, u0m, u0p, p, c0, d, a);
+        }
+        const int rb = r - 1;
+        const float w2 = __shfl_up_sync(FULL, v1m.w, 1), e2 = __shfl_down_sync(FULL, v1m.x, 1);
+        if (own && rb >= y0 && rb < ny) {
+            const int64_t rowb = (int64_t)rb * nx;
+            float d[4], a[4];
+            factors(rb, src2, a2, d, a);
+            const float4 v2 = fwd_row4(v1m, w2, e2, v1m2, v10, u0m, cm, d, a);
+            *reinterpret_cast<float4*>(u1 + rowb + i) = v1m;
+            *reinterpret_cast<float4*>(u2 + rowb + i) = v2;
+            if (ck1) *reinterpret_cast<float4*>(ck1 + rowb + i) = v1m;
+            if (ck2) *reinterpret_cast<float4*>(ck2 + rowb + i) = v2;
+        }
+        u0m = u00; u00 = u0p;
+        cm = c0;
+        v1m2 = v1m; v1m = v10;
+    }
+}
+
+template <int R>
+void fwd2q_strip(const DevGeo& g, const float* coef, const Fwd2Step& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    dim3 grid((g.nx + 119) / 120, (g.ny + rows_per_block - 1) / rows_per_block + 1, s.ng);
+    k_fwd2q_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+}
+
+template <int R>
+void fwd2_strip(const DevGeo& g, const float* coef, const Fwd2Step& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    dim3 grid((g.nx + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block + 1, s.ng);
+    k_fwd2_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+}
+
 template <int R>
 void fwd_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
@@ -407,6 +630,28 @@ void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, 
 }
 
 bool strip_supported(const DevGeo& g, int profile) { return profile == TOMO_PROFILE_CFG && g.nx % 4 == 0; }
+
+void launch_fwd2_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& a, const FwdStep& b,
+                       bool gather_prev, bool gather_cur, void* stream) {
+    Fwd2Step s{};
+    s.up = a.up; s.uc = a.uc; s.u1 = a.un; s.u2 = b.un; s.gstride = a.gstride;
+    s.ck1 = a.ck; s.ck2 = b.ck; s.ckstride = a.ck ? a.ckstride : b.ckstride;
+    s.k = a.k; s.g0 = a.g0; s.ng = a.ng;
+    s.gmeas = a.gmeas; s.gout = a.gout;
+    s.gka = (a.gout && gather_prev) ? a.k - 1 : -1;   // slice k-1, read from a.up
+    s.gkb = (a.gout && gather_cur) ? a.k : -1;        // slice k, read from a.uc
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (rows) {
+    case 4: fwd2_strip<4>(g, coef, s, st); break;
+    case 16: fwd2_strip<16>(g, coef, s, st); break;
+    case 32: fwd2_strip<32>(g, coef, s, st); break;
+    case 104: fwd2q_strip<4>(g, coef, s, st); break;
+    case 108: fwd2q_strip<8>(g, coef, s, st); break;
+    case 116: fwd2q_strip<16>(g, coef, s, st); break;
+    case 132: fwd2q_strip<32>(g, coef, s, st); break;
+    default: fwd2_strip<8>(g, coef, s, st); break;
+    }
+}
 
 void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& a, const AdjStep& b,
                        void* stream) {
