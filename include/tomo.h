@@ -217,6 +217,42 @@ tomo_status tomo_synchronize(tomo_ctx* ctx);
 tomo_status tomo_time_kernel(tomo_ctx* ctx, int32_t which, int32_t steps,
                              double* ms_per_launch, double* bytes_per_launch);
 
+/* ---- learned update (no reference counterpart: the reference's updates are
+ * hand-set step rules) --------------------------------------------------------
+ * A 5-layer 3x3 CNN, 32 channels, ReLU, BF16 weights/activations with FP32
+ * accumulation, reading per pixel (f, normalised SIRT direction, normalised
+ * illumination) and proposing a field update.  Feature tensors are planar FP32
+ * [B][3][H][W]; outputs [B][H][W]; W must be a multiple of 64. */
+typedef struct tomo_net tomo_net;
+int64_t     tomo_net_num_params(void);
+tomo_status tomo_net_create(int32_t device, uint64_t seed, tomo_net** out);
+void        tomo_net_destroy(tomo_net* net);
+const char* tomo_net_last_error(const tomo_net* net);
+tomo_status tomo_net_get_params(tomo_net* net, float* host);
+tomo_status tomo_net_set_params(tomo_net* net, const float* host);
+tomo_status tomo_net_save(tomo_net* net, const char* path);
+tomo_status tomo_net_load(tomo_net* net, const char* path);
+tomo_status tomo_net_forward_device(tomo_net* net, const float* d_feat, int32_t B, int32_t H, int32_t W,
+                                    float* d_out);
+/* Masked mean-squared-error gradient w.r.t. the parameters (binary mask). */
+tomo_status tomo_net_grad_device(tomo_net* net, const float* d_feat, const float* d_target, const float* d_mask,
+                                 int32_t B, int32_t H, int32_t W, float* host_grad, double* loss);
+/* One Adam step (beta 0.9/0.999) on the masked MSE. */
+tomo_status tomo_net_train_step_device(tomo_net* net, const float* d_feat, const float* d_target,
+                                       const float* d_mask, int32_t B, int32_t H, int32_t W, float lr,
+                                       double* loss);
+/* Features of the field d_f (device): planar [3][ny][nx] = f, the plain
+ * weighted-SIRT direction scaled to max 1 over the mask, the illumination
+ * sum_g sum_k u^2 scaled to max 1 over the mask.  Also returns the squared
+ * record residual at d_f.  The context's records must be set. */
+tomo_status tomo_features_device(tomo_ctx* ctx, const float* d_f, float* d_feat, double* resid_norm2);
+/* One learned iteration: the network proposes f + mask * net(features); the
+ * proposal is accepted only if the squared record residual decreases,
+ * otherwise the step falls back to plain weighted SIRT (TOMO_SIRT_NORM with
+ * `fallback`).  *accepted (optional) receives 1 or 0. */
+tomo_status tomo_iterate_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedule* fallback, int32_t iter,
+                                 float* d_f, const float* d_f_true, tomo_iter_stats* stats, int32_t* accepted);
+
 /* Forward solve without any device allocation (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc: applications whose own
  * pool allocator owns all device memory, or latency-bound loops where

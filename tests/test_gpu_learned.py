@@ -1,0 +1,131 @@
+"""GPU checks of the learned update: network kernels against the CPU reference
+(oracle/cnn_oracle.py, BF16 rounding emulated), training progress, features,
+and the residual-checked learned iteration with its plain-SIRT fallback.
+
+Tolerances: network output 5e-3 and parameter gradient 2e-2 relative L2 (the
+GPU and the reference round activations to BF16 at the same points; residual
+differences come from FP32 summation order flipping a few BF16 roundings)."""
+import numpy as np
+import pytest
+
+import cnn_oracle as K
+import oracle_lib as O
+import tomo
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def torch_dev(built_lib):
+    import torch
+
+    return torch, torch.device("cuda", 0)
+
+
+def random_batch(rng, B, H, W):
+    feat = np.stack([0.05 * rng.standard_normal((B, H, W)), rng.uniform(-1, 1, (B, H, W)),
+                     rng.uniform(0, 1, (B, H, W))], axis=1).astype(np.float32)
+    tgt = (0.02 * rng.standard_normal((B, H, W))).astype(np.float32)
+    mask = (rng.random((B, H, W)) > 0.2).astype(np.float32)
+    return feat, tgt, mask
+
+
+def test_forward_and_gradient_match_reference(torch_dev):
+    torch, dev = torch_dev
+    rng = np.random.default_rng(1)
+    B, H, W = 2, 9, 128
+    feat, tgt, mask = random_batch(rng, B, H, W)
+    net = tomo.Net(0, seed=3)
+    p = net.params()
+    p[-1] = 0.01                         # nonzero output bias
+    net.set_params(p)
+    d_feat = torch.from_numpy(feat).to(dev)
+    d_out = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+    net.forward_device(d_feat.data_ptr(), B, H, W, d_out.data_ptr())
+    out_ref, _ = K.forward(p.astype(np.float64), feat.astype(np.float64), emulate=True)
+    assert rel(d_out.cpu().numpy(), out_ref) <= 5e-3
+    d_tgt, d_mask = torch.from_numpy(tgt).to(dev), torch.from_numpy(mask).to(dev)   # keep alive
+    g, loss = net.grad_device(d_feat.data_ptr(), d_tgt.data_ptr(), d_mask.data_ptr(), B, H, W)
+    loss_ref, g_ref = K.loss_and_grad(p.astype(np.float64), feat.astype(np.float64), tgt, mask, emulate=True)
+    assert abs(loss - loss_ref) <= 1e-2 * loss_ref
+    # per layer, so a wrong layer cannot hide behind a large one
+    o = 0
+    for name, shp in K.SHAPES:
+        n = int(np.prod(shp))
+        if np.linalg.norm(g_ref[o:o + n]) > 0:
+            assert rel(g[o:o + n], g_ref[o:o + n]) <= 2e-2, name
+        o += n
+
+
+def test_training_reduces_loss(torch_dev):
+    torch, dev = torch_dev
+    rng = np.random.default_rng(2)
+    B, H, W = 4, 32, 64
+    feat, _, mask = random_batch(rng, B, H, W)
+    tgt = (0.1 * feat[:, 1] * feat[:, 2]).astype(np.float32)   # a learnable local map
+    net = tomo.Net(0, seed=5)
+    df, dt, dm = (torch.from_numpy(a).to(dev) for a in (feat, tgt, mask))
+    losses = [net.train_step_device(df.data_ptr(), dt.data_ptr(), dm.data_ptr(), B, H, W, 2e-3) for _ in range(150)]
+    assert losses[-1] < 0.2 * losses[0]
+
+
+def cfg_small():
+    return tomo.cfg_config(nx=128, ny=96, nt=260, n_transducers=32, group_size=8, radius=40.0,
+                           cells_per_wavelength=10.0, sponge_width=10)
+
+
+def test_features_and_fallback_equal_plain_norm_step(torch_dev):
+    torch, dev = torch_dev
+    cfg = cfg_small()
+    fo = tomo.phantom_cfg(cfg.nx, cfg.ny, 0, 3, 4, 9, 0.1, 0.0, 30.0, 11)
+    sched = tomo.schedule(omega=0.02, normalize=1)
+    with tomo.Context(cfg) as ctx:
+        rec = ctx.forward(fo)
+        ctx.set_records(rec)
+        f0 = np.zeros_like(fo)
+        d_f = torch.from_numpy(f0).to(dev)
+        d_feat = torch.empty((3, cfg.ny, cfg.nx), dtype=torch.float32, device=dev)
+        r2 = ctx.features_device(d_f.data_ptr(), d_feat.data_ptr())
+        feat = d_feat.cpu().numpy()
+        m = O.mask(cfg).astype(bool)
+        assert np.array_equal(feat[0], f0)
+        assert abs(np.abs(feat[1][m]).max() - 1.0) < 1e-6
+        assert abs(feat[2][m].max() - 1.0) < 1e-6 and feat[2].min() >= 0
+        # the direction feature is the plain weighted-SIRT step direction
+        f_plain = f0.copy()
+        st = ctx.iterate(tomo.SIRT_NORM, sched, 0, f_plain, None, fo)
+        assert r2 == st.resid_norm2
+        assert rel(f_plain[m] / 0.02, feat[1][m]) < 1e-6
+        # a network proposing nothing is rejected and the step falls back to plain SIRT
+        net = tomo.Net(0, seed=1)
+        net.set_params(np.zeros(net.n_params, np.float32))
+        d_ft = torch.from_numpy(fo).to(dev)
+        st2, acc = ctx.iterate_learned(net, sched, 0, d_f.data_ptr(), d_ft.data_ptr())
+        assert not acc
+        assert np.array_equal(d_f.cpu().numpy(), f_plain)
+        assert st2.epsilon == st.epsilon
+
+
+def test_learned_step_accepted_when_residual_drops(torch_dev):
+    torch, dev = torch_dev
+    cfg = cfg_small()
+    m = O.mask(cfg).astype(np.float32)
+    fo = (0.03 * m).astype(np.float32)          # the phantom is a constant over the mask
+    with tomo.Context(cfg) as ctx:
+        ctx.set_records(ctx.forward(fo))
+        net = tomo.Net(0, seed=1)
+        p = np.zeros(net.n_params, np.float32)
+        p[-1] = 0.03                             # the network proposes exactly the missing field
+        net.set_params(p)
+        d_f = torch.zeros(fo.shape, dtype=torch.float32, device=dev)
+        d_ft = torch.from_numpy(fo).to(dev)
+        st, acc = ctx.iterate_learned(net, tomo.schedule(omega=0.02, normalize=1), 0, d_f.data_ptr(),
+                                      d_ft.data_ptr())
+        assert acc
+        assert st.epsilon < 1e-3

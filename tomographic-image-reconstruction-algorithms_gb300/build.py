@@ -24,7 +24,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I" + INCLUDE, "-I" + CSRC]
 
-LIB_SOURCES = ["kernels.cu", "strip.cu", "engine.cu", "geometry.cpp", "noalloc.cu"]
+LIB_SOURCES = ["kernels.cu", "strip.cu", "engine.cu", "geometry.cpp", "noalloc.cu", "cnn.cu", "net.cu"]
 # driver name -> -D selector of cli/tomo_cli.cpp
 DRIVERS = {
     "generate-field": "GENERATE_FIELD",

@@ -70,6 +70,10 @@ struct tomo_ctx {
     int rows_adj2 = 8;
     bool fwd_pair = false;       // two forward steps per launch (needs S >= 4)
     int rows_fwd2 = 8;
+    // learned iteration (allocated on first use)
+    float *illum = nullptr, *feat = nullptr, *fsave = nullptr, *dnet = nullptr;
+    unsigned int* illum_max = nullptr;
+    bool illum_ready = false;
     static constexpr int ZR = 4; // adjoint ring slots
     bool tuned = false;
     std::vector<void*> allocs;
@@ -128,7 +132,9 @@ struct tomo_ctx {
 
 namespace {
 
-enum Mode { MODE_FWD = 0, MODE_GRAD = 1 };
+// FWD: simulated records; GRAD: residual + checkpoints + adjoint; RESID: residual only;
+// ILLUM: illumination sum of u^2 over all steps and groups
+enum Mode { MODE_FWD = 0, MODE_GRAD = 1, MODE_RESID = 2, MODE_ILLUM = 3 };
 
 void fwd_launch(tomo_ctx* c, const FwdStep& fs) {
     if (c->strip) launch_fwd_strip(c->rows_fwd, c->dg, c->coef, fs, c->st);
@@ -352,7 +358,16 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     launch_zero_slots(c->hist, ng, gstride, c->slot(0), c->slot(1), N, st);
     ++n;
     const float* meas_g = c->meas + (int64_t)g0 * rpg;
-    float* out_g = mode == MODE_GRAD ? c->rr : c->rec + (int64_t)g0 * rpg;
+    const bool resid = mode == MODE_GRAD || mode == MODE_RESID;
+    float* out_g = resid ? c->rr : c->rec + (int64_t)g0 * rpg;
+    if (mode == MODE_ILLUM) {
+        for (int k = 1; k <= nt - 2; ++k) {
+            fwd_launch(c, fwd_args(c, k, g0, ng));
+            launch_illum_add(c->hist + c->slot(k + 1), ng, gstride, N, c->illum, st);
+            n += 2;
+        }
+        return n;
+    }
     // checkpoint copy of slice m: chunk ch >= 1 starts at qa = 1 + ch*K and keeps slices qa-1 and qa
     auto ck_of = [&](FwdStep& fs, int m) {
         if (mode != MODE_GRAD || c->full) return;
@@ -370,7 +385,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         const int m = k + 1;
         ck_of(fs, m);
         if (c->strip) {
-            fs.gmeas = mode == MODE_GRAD ? meas_g : nullptr;
+            fs.gmeas = resid ? meas_g : nullptr;
             fs.gout = out_g;
             if (c->fwd_pair && k + 1 <= nt - 2) {
                 // slices k+1 and k+2; records slices k-1 and k from the launch's inputs
@@ -398,9 +413,9 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         gs.gstride = gstride;
         gs.k = m;
         gs.ng = ng;
-        gs.meas = mode == MODE_GRAD ? meas_g : nullptr;
+        gs.meas = resid ? meas_g : nullptr;
         gs.out = out_g;
-        gs.part = mode == MODE_GRAD ? c->rpart + (int64_t)g0 * nt : nullptr;
+        gs.part = resid ? c->rpart + (int64_t)g0 * nt : nullptr;
         launch_gather(c->dg, gs, st);
         n += 2;
         k += 1;
@@ -412,7 +427,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             gs.gstride = gstride;
             gs.k = m;
             gs.ng = ng;
-            gs.meas = mode == MODE_GRAD ? meas_g : nullptr;
+            gs.meas = resid ? meas_g : nullptr;
             gs.out = out_g;
             launch_gather(c->dg, gs, st);
             ++n;
@@ -424,16 +439,16 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         gs.gstride = gstride;
         gs.k = nt - 1;
         gs.ng = ng;
-        gs.meas = mode == MODE_GRAD ? meas_g : nullptr;
+        gs.meas = resid ? meas_g : nullptr;
         gs.out = out_g;
         launch_gather(c->dg, gs, st);
         ++n;
-        if (mode == MODE_GRAD) {
+        if (resid) {
             launch_resid_parts(c->rr, ng, nt, (int)nch, c->rpart + (int64_t)g0 * nt, st);
             ++n;
         }
     }
-    if (mode == MODE_FWD) return n;
+    if (mode != MODE_GRAD) return n;
     // ---- adjoint sweep, chunks in reverse
     cudaMemsetAsync(c->z, 0, sizeof(float) * tomo_ctx::ZR * N * ng, (cudaStream_t)st);
     cudaMemsetAsync(c->corr + (int64_t)g0 * N, 0, sizeof(float) * N * ng, (cudaStream_t)st);
@@ -674,6 +689,66 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
     return TOMO_OK;
 }
 
+// Plain weighted (normalised) SIRT direction into c->dir from the correlations of
+// c->f (sirt-mimo-norm.cu:56-118, the same rule as TOMO_SIRT_NORM).
+tomo_status norm_direction(tomo_ctx* c) {
+    const Geometry& g = c->geo;
+    const int64_t N = g.N;
+    const int G = g.G, nb = reduce_blocks();
+    const double sc = g.corr_scale;
+    launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->tmp, c->st);
+    launch_group_dev_norm(c->corr, G, N, c->f, sc, c->tmp, c->part, nb, c->st);
+    launch_sum_parts(c->part, G, nb, c->sums, c->st);
+    std::vector<double> d2(G), w(G);
+    CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    double W = 0.0;
+    for (int gg = 0; gg < G; ++gg) { w[gg] = 1.0 / std::sqrt(d2[gg]); W += w[gg]; }
+    for (int gg = 0; gg < G; ++gg) w[gg] /= W;
+    CU(c, cudaMemcpyAsync(c->sums, w.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
+    launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
+    CU(c, cudaStreamSynchronize(c->st));
+    c->launches += 4;
+    return TOMO_OK;
+}
+
+tomo_status ensure_learned_buffers(tomo_ctx* c) {
+    if (c->feat) return TOMO_OK;
+    const int64_t N = c->geo.N;
+    TRY(c->alloc(&c->illum, N, "illumination"));
+    TRY(c->alloc(&c->feat, 3 * N, "features"));
+    TRY(c->alloc(&c->fsave, N, "saved field"));
+    TRY(c->alloc(&c->dnet, N, "network update"));
+    TRY(c->alloc(&c->illum_max, 1, "illumination max"));
+    return TOMO_OK;
+}
+
+// Illumination sum_g sum_k u_g(k)^2 of the field currently in c->f, once per context.
+tomo_status compute_illumination(tomo_ctx* c) {
+    if (c->illum_ready) return TOMO_OK;
+    const Geometry& g = c->geo;
+    CU(c, cudaMemsetAsync(c->illum, 0, sizeof(float) * g.N, c->st));
+    launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
+    for (int g0 = 0; g0 < g.G; g0 += c->P) TRY(run_pass(c, MODE_ILLUM, g0, std::min(c->P, g.G - g0)));
+    launch_maxabs(c->illum, c->mask, g.N, c->illum_max, c->st);
+    CU(c, cudaStreamSynchronize(c->st));
+    c->illum_ready = true;
+    return TOMO_OK;
+}
+
+// Features of c->f into c->feat; the direction stays in c->dir and its maximum in c->maxabs.
+tomo_status features_core(tomo_ctx* c, double* r2) {
+    TRY(ensure_learned_buffers(c));
+    TRY(compute_illumination(c));
+    TRY(gradient_all(c));
+    TRY(residual_norm(c, r2));
+    TRY(norm_direction(c));
+    launch_maxabs(c->dir, c->mask, c->geo.N, c->maxabs, c->st);
+    launch_features(c->f, c->dir, c->maxabs, c->illum, c->illum_max, c->geo.N, c->feat, c->st);
+    c->launches += 2;
+    return TOMO_OK;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -910,6 +985,72 @@ tomo_status tomo_iterate_device(tomo_ctx* c, int32_t method, const tomo_schedule
     if (d_f_true) CU(c, cudaMemcpyAsync(c->ftrue, d_f_true, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
     TRY(iterate_core(c, method, sched, iter, d_f_true != nullptr, stats));
     CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    return TOMO_OK;
+}
+
+tomo_status tomo_features_device(tomo_ctx* c, const float* d_f, float* d_feat, double* resid_norm2) {
+    if (!c || !d_f || !d_feat) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
+    CU(c, cudaSetDevice(c->dev));
+    const int64_t N = c->geo.N;
+    CU(c, cudaMemcpyAsync(c->f, d_f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+    double r2 = 0.0;
+    TRY(features_core(c, &r2));
+    CU(c, cudaMemcpyAsync(d_feat, c->feat, sizeof(float) * 3 * N, cudaMemcpyDeviceToDevice, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    if (resid_norm2) *resid_norm2 = r2;
+    return TOMO_OK;
+}
+
+tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fallback, int32_t iter, float* d_f,
+                                 const float* d_f_true, tomo_iter_stats* stats, int32_t* accepted) {
+    if (!c || !net || !fallback || !d_f) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
+    CU(c, cudaSetDevice(c->dev));
+    const Geometry& g = c->geo;
+    const int64_t N = g.N;
+    const double s = sched_scale(fallback, iter);
+    if (!std::isfinite(s)) return c->fail(TOMO_ERR_ARG, "bad schedule");
+    const int64_t launches0 = c->launches;
+    CU(c, cudaMemcpyAsync(c->f, d_f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+    if (d_f_true) CU(c, cudaMemcpyAsync(c->ftrue, d_f_true, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+    CU(c, cudaEventRecord(c->ev0, c->st));
+    double r0 = 0.0, r1 = 0.0;
+    TRY(features_core(c, &r0));
+    // proposal f + mask * net(features)
+    tomo_status ns = net_infer(net, c->feat, g.ny, g.nx, c->dnet, c->st);
+    if (ns != TOMO_OK) return c->fail(ns, "network: %s", tomo_net_last_error(net));
+    c->launches += 6;
+    CU(c, cudaMemcpyAsync(c->fsave, c->f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+    launch_apply(c->f, c->dnet, c->mask, N, 1.0, nullptr, c->st);
+    launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
+    c->launches += 2;
+    for (int g0 = 0; g0 < g.G; g0 += c->P) TRY(run_pass(c, MODE_RESID, g0, std::min(c->P, g.G - g0)));
+    TRY(residual_norm(c, &r1));
+    const bool ok = r1 < r0;
+    if (!ok) {
+        // plain weighted SIRT step from the saved field along its direction
+        CU(c, cudaMemcpyAsync(c->f, c->fsave, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+        launch_apply(c->f, c->dir, c->mask, N, s, fallback->normalize ? c->maxabs : nullptr, c->st);
+        ++c->launches;
+    }
+    CU(c, cudaEventRecord(c->ev1, c->st));
+    double eps = std::numeric_limits<double>::quiet_NaN();
+    if (d_f_true) TRY(epsilon(c, &eps));
+    CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    CU(c, cudaGetLastError());
+    if (accepted) *accepted = ok ? 1 : 0;
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        stats->epsilon = eps;
+        stats->resid_norm2 = r0;
+        stats->scale = ok ? 1.0 : s;
+        stats->seconds = ms * 1e-3;
+        stats->cell_updates = 3.0 * (double)g.G * (double)(g.nt - 2) * (double)N;
+        stats->kernel_launches = (double)(c->launches - launches0);
+    }
     return TOMO_OK;
 }
 

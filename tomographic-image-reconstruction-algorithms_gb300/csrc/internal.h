@@ -150,6 +150,11 @@ void launch_apply(float* f, const float* dir, const uint8_t* mask, int64_t N, do
 void launch_eps_parts(const float* f, const float* fo, int64_t N, double* part, int nb, void* stream);
 
 int reduce_blocks();  // number of partial blocks the reductions use
+void launch_illum_add(const float* u, int ng, int64_t gstride, int64_t N, float* I, void* stream);
+void launch_features(const float* f, const float* dir, const unsigned int* dmax, const float* I, const unsigned int* imax,
+                     int64_t N, float* feat, void* stream);
+// learned update network (net.cu): one image, features planar [3][H][W], output [H][W]
+tomo_status net_infer(tomo_net* net, const float* feat, int H, int W, float* out, void* stream);
 
 // warp-strip step kernels (strip.cu): CFG profile, nx % 4 == 0; rows per warp in {2,4,8,16,32}
 bool strip_supported(const DevGeo& g, int profile);

@@ -377,6 +377,30 @@ __global__ void __launch_bounds__(RED_THREADS) k_eps_parts(const float* __restri
     block_store_sum(b, part + gridDim.x + blockIdx.x);
 }
 
+// Illumination: I[q] += sum over the pass's groups of u[q]^2 (group order fixed).
+__global__ void k_illum_add(const float* __restrict__ u, int ng, int64_t gstride, int64_t N, float* __restrict__ I) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N; q += (int64_t)gridDim.x * blockDim.x) {
+        float acc = I[q];
+        for (int gl = 0; gl < ng; ++gl) {
+            const float v = u[gl * gstride + q];
+            acc = fmaf(v, v, acc);
+        }
+        I[q] = acc;
+    }
+}
+
+// Network features, planar [3][N]: f, dir / max|dir|, I / max I (maxima over the mask).
+__global__ void k_features(const float* __restrict__ f, const float* __restrict__ dir, const unsigned int* dmax,
+                           const float* __restrict__ I, const unsigned int* imax, int64_t N, float* __restrict__ feat) {
+    const float dm = __uint_as_float(*dmax), im = __uint_as_float(*imax);
+    const float ds = dm > 0.f ? 1.f / dm : 0.f, is = im > 0.f ? 1.f / im : 0.f;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N; q += (int64_t)gridDim.x * blockDim.x) {
+        feat[q] = f[q];
+        feat[N + q] = dir[q] * ds;
+        feat[2 * N + q] = I[q] * is;
+    }
+}
+
 inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
 inline int grid1(int64_t n, int t) {
     const int64_t b = (n + t - 1) / t;
@@ -409,6 +433,15 @@ void launch_gather(const DevGeo& g, const GatherStep& s, void* st) {
 }
 
 void launch_fill(float* p, int64_t n, float v, void* st) { k_fill<<<grid1(n, 256), 256, 0, S(st)>>>(p, n, v); }
+
+void launch_illum_add(const float* u, int ng, int64_t gstride, int64_t N, float* I, void* st) {
+    k_illum_add<<<grid1(N, 256), 256, 0, S(st)>>>(u, ng, gstride, N, I);
+}
+
+void launch_features(const float* f, const float* dir, const unsigned int* dmax, const float* I, const unsigned int* imax,
+                     int64_t N, float* feat, void* st) {
+    k_features<<<grid1(N, 256), 256, 0, S(st)>>>(f, dir, dmax, I, imax, N, feat);
+}
 
 void launch_zero_slots(float* base, int ng, int64_t gstride, int64_t off0, int64_t off1, int64_t N, void* st) {
     const int bx = (int)((N + 255) / 256 < 64 ? (N + 255) / 256 : 64);

@@ -160,6 +160,19 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_synchronize": (i32, [vp]),
         "tomo_time_kernel": (i32, [vp, i32, i32, DP, DP]),
         "tomo_forward_noalloc": (i32, [C.POINTER(Config), vp, vp, vp]),
+        "tomo_net_num_params": (C.c_int64, []),
+        "tomo_net_create": (i32, [i32, u64, C.POINTER(vp)]),
+        "tomo_net_destroy": (None, [vp]),
+        "tomo_net_last_error": (C.c_char_p, [vp]),
+        "tomo_net_get_params": (i32, [vp, FP]),
+        "tomo_net_set_params": (i32, [vp, FP]),
+        "tomo_net_save": (i32, [vp, C.c_char_p]),
+        "tomo_net_load": (i32, [vp, C.c_char_p]),
+        "tomo_net_forward_device": (i32, [vp, vp, i32, i32, i32, vp]),
+        "tomo_net_grad_device": (i32, [vp, vp, vp, vp, i32, i32, i32, FP, DP]),
+        "tomo_net_train_step_device": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, DP]),
+        "tomo_features_device": (i32, [vp, vp, vp, DP]),
+        "tomo_iterate_learned": (i32, [vp, vp, C.POINTER(Schedule), i32, vp, vp, C.POINTER(IterStats), IP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -306,6 +319,75 @@ class Context:
     def synchronize(self):
         self._check(lib().tomo_synchronize(self.h))
 
+    def features_device(self, d_f: int, d_feat: int) -> float:
+        """Writes the network features of the device field d_f into d_feat (3*ny*nx floats)."""
+        r2 = C.c_double()
+        self._check(lib().tomo_features_device(self.h, C.c_void_p(d_f), C.c_void_p(d_feat), C.byref(r2)))
+        return r2.value
+
+    def iterate_learned(self, net: "Net", fallback: Schedule, it: int, d_f: int, d_ftrue: int = 0):
+        """One residual-checked learned iteration on the device field d_f; (stats, accepted)."""
+        stats = IterStats()
+        acc = C.c_int32()
+        self._check(lib().tomo_iterate_learned(self.h, net.h, C.byref(fallback), it, C.c_void_p(d_f),
+                                               C.c_void_p(d_ftrue or None), C.byref(stats), C.byref(acc)))
+        return stats, bool(acc.value)
+
     @property
     def stream(self) -> int:
         return lib().tomo_stream(self.h) or 0
+
+
+class Net:
+    """The learned update network (tomo_net): 5 layers of 3x3 convolutions."""
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        h = C.c_void_p()
+        st = lib().tomo_net_create(device, seed, C.byref(h))
+        if st:
+            raise TomoError(st, "tomo_net_create")
+        self.h = h
+        self.n_params = int(lib().tomo_net_num_params())
+
+    def _check(self, st):
+        if st:
+            raise TomoError(st, (lib().tomo_net_last_error(self.h) or b"").decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().tomo_net_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, np.float32)
+        self._check(lib().tomo_net_get_params(self.h, _fp(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        self._check(lib().tomo_net_set_params(self.h, _fp(p)))
+
+    def save(self, path: str):
+        self._check(lib().tomo_net_save(self.h, path.encode()))
+
+    def load(self, path: str):
+        self._check(lib().tomo_net_load(self.h, path.encode()))
+
+    def forward_device(self, d_feat: int, B: int, H: int, W: int, d_out: int):
+        self._check(lib().tomo_net_forward_device(self.h, C.c_void_p(d_feat), B, H, W, C.c_void_p(d_out)))
+
+    def grad_device(self, d_feat: int, d_tgt: int, d_mask: int, B: int, H: int, W: int):
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_double()
+        self._check(lib().tomo_net_grad_device(self.h, C.c_void_p(d_feat), C.c_void_p(d_tgt), C.c_void_p(d_mask),
+                                               B, H, W, _fp(g), C.byref(loss)))
+        return g, loss.value
+
+    def train_step_device(self, d_feat: int, d_tgt: int, d_mask: int, B: int, H: int, W: int, lr: float) -> float:
+        loss = C.c_double()
+        self._check(lib().tomo_net_train_step_device(self.h, C.c_void_p(d_feat), C.c_void_p(d_tgt),
+                                                     C.c_void_p(d_mask), B, H, W, lr, C.byref(loss)))
+        return loss.value
