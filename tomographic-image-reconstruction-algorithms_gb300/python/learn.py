@@ -1,0 +1,199 @@
+"""Training and evaluation of the learned update (the 5-layer CNN in libtomo.so).
+
+Pipeline, all compute in libtomo.so's kernels (torch only holds device buffers):
+  1. data: seeded 256x256 ellipse phantoms (8 ellipses, axes 5..30 cells,
+     f in U[-0.15, 0.15], smoothed noise 0.01), the 512x512 workload's physics
+     scaled to 256x256 (nt 1250, 128 transducers on radius 110, groups of 8,
+     1% record noise).  Plain weighted SIRT (normalised-weight direction,
+     step `STEP` along the direction scaled to max 1) runs `iters` iterations
+     per phantom; iteration t gives the pair
+        features (f_t, direction_t, illumination)  ->  target  f_{t+K} - f_t
+     the field change of the next K plain steps (the look-ahead K defaults to
+     6): the network learns to jump ahead along the plain trajectory.
+  2. training: Adam on the masked mean squared error, on the GPU.
+  3. evaluation (time to image): on the 512x512 workload, plain weighted SIRT
+     runs `plain_iters` iterations; the learned iteration (network proposal
+     accepted only when the record residual drops, else the plain step) runs
+     until it reaches the plain method's final image error.
+
+Usage:  python learn.py [--phantoms 1000] [--iters 20] [--epochs 8] [--out weights.bin]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import tomo  # noqa: E402
+
+STEP = 0.02          # plain weighted SIRT step (direction scaled to max 1 over the mask)
+WEIGHTS = os.path.join(tomo.PKG_DIR, "weights", "learned_update.bin")
+
+
+def train_config(device=0):
+    return tomo.cfg_config(nx=256, ny=256, nt=1250, n_transducers=128, group_size=8, radius=110.0,
+                           ckpt_interval=0, device=device)
+
+
+def eval_config(device=0):
+    return tomo.cfg_config(nx=512, ny=512, nt=2500, n_transducers=256, group_size=8, radius=220.0,
+                           ckpt_interval=50, device=device)
+
+
+def phantom(cfg, seed, rmin, rmax):
+    return tomo.phantom_cfg(cfg.nx, cfg.ny, 1, 8, rmin, rmax, 0.15, 0.01, 0.8 * cfg.radius, seed)
+
+
+def mask_of(cfg):
+    y, x = np.mgrid[0:cfg.ny, 0:cfg.nx]
+    r = cfg.radius - 1.5
+    return (((x - 0.5 * cfg.nx) ** 2 + (y - 0.5 * cfg.ny) ** 2) < r * r).astype(np.float32)
+
+
+def generate(n_phantoms, iters, lookahead=6, seed0=4000, device=0, log=print):
+    """Plain weighted SIRT trajectories -> (features [M,3,H,W], targets [M,H,W], mask [H,W]) on the GPU,
+    M = n_phantoms * (iters - lookahead + 1)."""
+    import torch
+
+    dev = torch.device("cuda", device)
+    cfg = train_config(device)
+    m = torch.from_numpy(mask_of(cfg)).to(dev)
+    per = iters - lookahead + 1
+    M = n_phantoms * per
+    feats = torch.empty((M, 3, cfg.ny, cfg.nx), dtype=torch.float32, device=dev)
+    tgts = torch.empty((M, cfg.ny, cfg.nx), dtype=torch.float32, device=dev)
+    traj = torch.empty((iters + 1, cfg.ny, cfg.nx), dtype=torch.float32, device=dev)
+    feat_t = torch.empty((iters, 3, cfg.ny, cfg.nx), dtype=torch.float32, device=dev)
+    t0 = time.time()
+    j = 0
+    with tomo.Context(cfg) as ctx:
+        for ph in range(n_phantoms):
+            fo = phantom(cfg, seed0 + ph, 5.0, 30.0)
+            ctx.set_records(ctx.generate_data(fo, noise_level=0.01, seed=seed0 + ph))
+            traj[0].zero_()
+            for it in range(iters):
+                torch.cuda.synchronize(dev)   # torch writes the trajectory on its own stream
+                ctx.features_device(traj[it].data_ptr(), feat_t[it].data_ptr())
+                traj[it + 1] = traj[it] + STEP * m * feat_t[it, 1]      # the plain weighted SIRT step
+            feats[j:j + per] = feat_t[:per]
+            tgts[j:j + per] = traj[lookahead:lookahead + per] - traj[:per]
+            j += per
+            if ph % 100 == 0:
+                log(f"  data: phantom {ph}/{n_phantoms}, {time.time() - t0:.1f} s")
+    torch.cuda.synchronize(dev)
+    return feats, tgts, m, time.time() - t0
+
+
+def train(net, feats, tgts, mask, epochs, batch=16, lr=1e-3, seed=0, log=print):
+    import torch
+
+    M, _, H, W = feats.shape
+    bm = mask.expand(batch, H, W).contiguous()
+    rng = np.random.default_rng(seed)
+    steps = epochs * (M // batch)
+    t0 = time.time()
+    s = 0
+    losses = []
+    for ep in range(epochs):
+        perm = torch.from_numpy(rng.permutation(M)).to(feats.device)
+        acc = 0.0
+        for b in range(M // batch):
+            idx = perm[b * batch:(b + 1) * batch]
+            fb = feats[idx].contiguous()
+            tb = tgts[idx].contiguous()
+            torch.cuda.synchronize(feats.device)
+            cur = lr * 0.5 * (1 + np.cos(np.pi * s / steps))      # cosine decay
+            acc += net.train_step_device(fb.data_ptr(), tb.data_ptr(), bm.data_ptr(), batch, H, W, cur)
+            s += 1
+        losses.append(acc / (M // batch))
+        log(f"  epoch {ep}: loss {losses[-1]:.3e}, {time.time() - t0:.1f} s")
+    return losses, time.time() - t0
+
+
+def time_to_image(net, plain_iters=30, seed=2001, device=0, log=print):
+    """Plain weighted SIRT for plain_iters iterations vs the learned iteration to the same image error."""
+    import torch
+
+    dev = torch.device("cuda", device)
+    cfg = eval_config(device)
+    fo = phantom(cfg, seed, 10.0, 60.0)
+    sched = tomo.schedule(omega=STEP, normalize=1)
+    out = {}
+    with tomo.Context(cfg) as ctx:
+        rec = ctx.generate_data(fo, noise_level=0.01, seed=77)
+        d_fo = torch.from_numpy(fo).to(dev)
+        d_rec = torch.from_numpy(rec).to(dev)
+        d_f = torch.zeros_like(d_fo)
+        torch.cuda.synchronize(dev)
+        ctx.iterate_device(tomo.SIRT_NORM, sched, 0, d_f.data_ptr(), d_rec.data_ptr(), d_fo.data_ptr())
+        d_f.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eps = []
+        for it in range(plain_iters):
+            st = ctx.iterate_device(tomo.SIRT_NORM, sched, it, d_f.data_ptr(), 0, d_fo.data_ptr())
+            eps.append(st.epsilon)
+        ctx.synchronize()
+        t_plain = time.perf_counter() - t0
+        target = eps[-1]
+        log(f"  plain: {plain_iters} iterations, eps {eps[0]:.3f} -> {target:.3f} %, {t_plain:.3f} s")
+        d_f.zero_()
+        torch.cuda.synchronize(dev)
+        ctx.iterate_learned(net, sched, 0, d_f.data_ptr(), d_fo.data_ptr())   # warm up (illumination, graphs)
+        d_f.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        leps, accepted = [], 0
+        for it in range(3 * plain_iters):
+            st, acc = ctx.iterate_learned(net, sched, it, d_f.data_ptr(), d_fo.data_ptr())
+            leps.append(st.epsilon)
+            accepted += int(acc)
+            if st.epsilon <= target:
+                break
+        ctx.synchronize()
+        t_learned = time.perf_counter() - t0
+        log(f"  learned: {len(leps)} iterations ({accepted} accepted), eps -> {leps[-1]:.3f} %, {t_learned:.3f} s")
+        out = {"plain_iters": plain_iters, "plain_seconds": t_plain, "plain_final_epsilon": target,
+               "plain_epsilon": eps, "learned_iters": len(leps), "learned_accepted": accepted,
+               "learned_seconds": t_learned, "learned_final_epsilon": leps[-1], "learned_epsilon": leps,
+               "reached": leps[-1] <= target, "speedup": t_plain / t_learned if leps[-1] <= target else None}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--phantoms", type=int, default=1000)
+    ap.add_argument("--iters", type=int, default=26)
+    ap.add_argument("--lookahead", type=int, default=6)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--eval-only", action="store_true")
+    args = ap.parse_args()
+    net = tomo.Net(0, seed=7)
+    report = {}
+    if not args.eval_only:
+        feats, tgts, m, t_data = generate(args.phantoms, args.iters, args.lookahead)
+        report["lookahead"] = args.lookahead
+        report["pairs"] = int(feats.shape[0])
+        report["data_seconds"] = t_data
+        losses, t_train = train(net, feats, tgts, m, args.epochs, args.batch, args.lr)
+        report["losses"] = losses
+        report["train_seconds"] = t_train
+        os.makedirs(os.path.dirname(args.out), exist_ok=True)
+        net.save(args.out)
+        del feats, tgts
+    else:
+        net.load(args.out)
+    report["time_to_image"] = time_to_image(net)
+    print(json.dumps(report))
+
+
+if __name__ == "__main__":
+    main()
