@@ -199,6 +199,19 @@ def metric_name():
     return "stencil GB/s (algorithmic 36 B per forward+adjoint cell-update) of one plain weighted SIRT iteration"
 
 
+def read_tuning(path):
+    """The strip-kernel choice of the autotuner, from its cache file (last line)."""
+    try:
+        lines = [l.split() for l in open(path) if l.startswith("tomo-tune-1")]
+    except OSError:
+        return None
+    if not lines:
+        return None
+    v = [int(x) for x in lines[-1][7:14]]
+    return {"fwd": f"two steps/launch, code {v[6]}" if v[5] else f"one step/launch, {v[0]} rows",
+            "adj": f"two steps/launch, {v[4]} rows" if v[3] else f"one step/launch, {v[1]} rows, variant {v[2]}"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -245,9 +258,14 @@ def main():
         G0 = tomo.n_groups(cfg)
         cpu = cpu_sample(w, cfg, fo, np.zeros((G0, cfg.nt, tomo.n_channels(cfg)), np.float32))
 
+    # the kernel choice is recorded in a tuning cache (reused when TOMO_TUNE_CACHE names one)
+    own_cache = not os.environ.get("TOMO_TUNE_CACHE")
+    if own_cache:
+        os.environ["TOMO_TUNE_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="tomo_tune_"), "tune.txt")
     ctx = tomo.Context(cfg)
     G = ctx.G
     rec = ctx.generate_data(fo, noise_level=w["noise"], seed=77 + rank)
+    tuning = read_tuning(os.environ["TOMO_TUNE_CACHE"])
     sched = tomo.schedule(**w["sched"])
     dev = torch.device("cuda", local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
@@ -272,12 +290,14 @@ def main():
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        torch.cuda.nvtx.range_push("timed_steps")     # lets ncu --nvtx-include select the timed region
         e0.record(stream)
         for s in range(args.steps):
             st = ctx.iterate_device(w["method"], sched, args.warmup + s, d_f.data_ptr(), 0, d_ft.data_ptr())
             launches += st.kernel_launches
             eps.append(st.epsilon)
         e1.record(stream)
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize(dev)
     barrier()
     ms = e0.elapsed_time(e1)
@@ -339,7 +359,8 @@ def main():
             "config": {"workload": args.workload + ": " + w["desc"], "groups": G,
                        "groups_per_pass": info.groups_per_pass, "ckpt_interval": K,
                        "l2": "inputs larger than L2 (%.1f GB resident working set)" % (info.device_bytes / 1e9),
-                       "parallelism": f"replicas{world}" if world > 1 else "single GPU"},
+                       "parallelism": f"replicas{world}" if world > 1 else "single GPU",
+                       "strip_kernels": tuning},
             "sirt_iter_per_s": world * args.steps / (t_max * 1e-3),
             "cell_updates_per_s": world * 2.0 * G * cfg.nx * cfg.ny * (nt - 2) * args.steps / (t_max * 1e-3),
             "epsilon_last": eps[-1] if eps else None,

@@ -252,6 +252,23 @@ tomo_status tomo_features_device(tomo_ctx* ctx, const float* d_f, float* d_feat,
  * `fallback`).  *accepted (optional) receives 1 or 0. */
 tomo_status tomo_iterate_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedule* fallback, int32_t iter,
                                  float* d_f, const float* d_f_true, tomo_iter_stats* stats, int32_t* accepted);
+/* Learned iterations on the device field d_f until the image error against
+ * d_f_true (optional) reaches target_epsilon (percent) or max_iters.  Each
+ * iteration proposes f + mask * net(features); the gradient sweep of the
+ * proposal is its residual check and, when it passes, also the next
+ * iteration's gradient, so an accepted step costs one gradient sweep.  The
+ * check passes when the squared record residual of the proposal is below the
+ * largest residual of the last `window` fields (1: below the current field's;
+ * 2 admits the period-two alternation of plain SIRT's own residual; 1..64).  A
+ * rejected proposal falls back to the plain weighted-SIRT step from the saved
+ * field (TOMO_SIRT_NORM with `fallback`).  Per iteration eps_log gets the image
+ * error (NaN without d_f_true) and accepted_log 1 or 0 (both optional, at least
+ * max_iters entries); *seconds is the host wall time of the loop after the
+ * one-off illumination sweep.  The counterpart of tomo_run for the learned
+ * update; the reference has none. */
+tomo_status tomo_run_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedule* fallback, float* d_f,
+                             const float* d_f_true, double target_epsilon, int32_t max_iters, int32_t window,
+                             double* eps_log, int32_t* accepted_log, int32_t* iters_done, double* seconds);
 
 /* Forward solve without any device allocation (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc: applications whose own

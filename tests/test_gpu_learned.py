@@ -129,3 +129,45 @@ def test_learned_step_accepted_when_residual_drops(torch_dev):
                                       d_ft.data_ptr())
         assert acc
         assert st.epsilon < 1e-3
+
+
+def test_run_learned_rejecting_network_is_plain_sirt(torch_dev):
+    """A network proposing nothing never lowers the residual: every proposal is
+    rejected and the run is plain weighted SIRT, bitwise."""
+    torch, dev = torch_dev
+    cfg = cfg_small()
+    fo = tomo.phantom_cfg(cfg.nx, cfg.ny, 0, 3, 4, 9, 0.1, 0.0, 30.0, 12)
+    sched = tomo.schedule(omega=0.02, normalize=1)
+    with tomo.Context(cfg) as ctx:
+        ctx.set_records(ctx.forward(fo))
+        f_plain = np.zeros_like(fo)
+        eps_plain = [ctx.iterate(tomo.SIRT_NORM, sched, it, f_plain, None, fo).epsilon for it in range(4)]
+        net = tomo.Net(0, seed=1)
+        net.set_params(np.zeros(net.n_params, np.float32))
+        d_f = torch.zeros(fo.shape, dtype=torch.float32, device=dev)
+        d_ft = torch.from_numpy(fo).to(dev)
+        eps, acc, secs = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), -1.0, 4)
+        assert len(eps) == 4 and not acc.any() and secs > 0
+        assert np.array_equal(d_f.cpu().numpy(), f_plain)
+        assert list(eps) == eps_plain
+
+
+def test_run_learned_stops_at_target(torch_dev):
+    torch, dev = torch_dev
+    cfg = cfg_small()
+    m = O.mask(cfg).astype(np.float32)
+    fo = (0.03 * m).astype(np.float32)
+    with tomo.Context(cfg) as ctx:
+        ctx.set_records(ctx.forward(fo))
+        net = tomo.Net(0, seed=1)
+        p = np.zeros(net.n_params, np.float32)
+        p[-1] = 0.03                             # the network proposes exactly the missing field
+        net.set_params(p)
+        d_f = torch.zeros(fo.shape, dtype=torch.float32, device=dev)
+        d_ft = torch.from_numpy(fo).to(dev)
+        eps, acc, _ = ctx.run_learned(net, tomo.schedule(omega=0.02, normalize=1), d_f.data_ptr(),
+                                      d_ft.data_ptr(), 1e-2, 10)
+        assert len(eps) == 1 and acc[0] and eps[0] < 1e-2
+        with pytest.raises(tomo.TomoError):
+            ctx.run_learned(net, tomo.schedule(omega=0.02, normalize=1), d_f.data_ptr(), d_ft.data_ptr(),
+                            1e-2, 10, window=0)

@@ -71,8 +71,8 @@ struct tomo_ctx {
     bool fwd_pair = false;       // two forward steps per launch (needs S >= 4)
     int rows_fwd2 = 8;
     // learned iteration (allocated on first use)
-    float *illum = nullptr, *feat = nullptr, *fsave = nullptr, *dnet = nullptr;
-    unsigned int* illum_max = nullptr;
+    float *illum = nullptr, *feat = nullptr, *fsave = nullptr, *dnet = nullptr, *dsave = nullptr;
+    unsigned int *illum_max = nullptr, *maxsave = nullptr;
     bool illum_ready = false;
     static constexpr int ZR = 4; // adjoint ring slots
     bool tuned = false;
@@ -178,11 +178,52 @@ AdjStep adj_args(tomo_ctx* c, int q, int g0, int ng) {
     return as;
 }
 
-// Picks rows per warp of the strip kernels by timing each candidate on this
-// problem (a few mid-sweep steps of the first pass); TOMO_STRIP_ROWS=<n> fixes it.
+// Tuning cache line: problem key, then the choices.
+std::string tune_key(const tomo_ctx* c) {
+    char b[160];
+    std::snprintf(b, sizeof b, "tomo-tune-1 %d %d %d %d %d %d", c->geo.cfg.profile, c->geo.nx, c->geo.ny, c->geo.nt,
+                  c->P, c->S);
+    return b;
+}
+
+bool tune_cache_read(tomo_ctx* c, const char* path) {
+    FILE* fp = std::fopen(path, "r");
+    if (!fp) return false;
+    const std::string key = tune_key(c);
+    char line[512];
+    bool hit = false;
+    while (!hit && std::fgets(line, sizeof line, fp)) {
+        if (std::strncmp(line, key.c_str(), key.size()) != 0 || line[key.size()] != ' ') continue;
+        int v[7];
+        if (std::sscanf(line + key.size(), "%d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5],
+                        &v[6]) == 7) {
+            c->rows_fwd = v[0]; c->rows_adj = v[1]; c->adj_variant = v[2]; c->adj_pair = v[3] != 0;
+            c->rows_adj2 = v[4]; c->fwd_pair = v[5] != 0 && c->S >= 4; c->rows_fwd2 = v[6];
+            hit = true;
+        }
+    }
+    std::fclose(fp);
+    return hit;
+}
+
+void tune_cache_append(const tomo_ctx* c, const char* path) {
+    FILE* fp = std::fopen(path, "a");
+    if (!fp) return;
+    std::fprintf(fp, "%s %d %d %d %d %d %d %d\n", tune_key(c).c_str(), c->rows_fwd, c->rows_adj, c->adj_variant,
+                 c->adj_pair ? 1 : 0, c->rows_adj2, c->fwd_pair ? 1 : 0, c->rows_fwd2);
+    std::fclose(fp);
+}
+
+// Picks the strip kernels (rows per warp, register variant, one or two steps
+// per launch) by timing each candidate on this problem (mid-sweep steps of the
+// first pass, best of three timed passes).  TOMO_STRIP_ROWS=<n> fixes the
+// choice; TOMO_TUNE_CACHE=<file> reuses a choice recorded there for the same
+// problem shape, or records the one made here.
 tomo_status autotune(tomo_ctx* c) {
     if (c->tuned || !c->strip) { c->tuned = true; return TOMO_OK; }
     c->tuned = true;
+    const char* cache = std::getenv("TOMO_TUNE_CACHE");
+    if (cache && *cache && tune_cache_read(c, cache)) return TOMO_OK;
     if (const char* e = std::getenv("TOMO_STRIP_ROWS")) {
         c->rows_fwd = c->rows_adj = c->rows_adj2 = std::atoi(e);
         if (const char* v = std::getenv("TOMO_ADJ_VARIANT")) c->adj_variant = std::atoi(v);
@@ -193,15 +234,17 @@ tomo_status autotune(tomo_ctx* c) {
         return TOMO_OK;
     }
     const int cands[5] = {2, 4, 8, 16, 32};
-    const int nt = c->geo.nt, ng = c->P, reps = 6;
-    const int k0 = std::max(1, nt / 2 - reps);
+    const int nt = c->geo.nt, ng = c->P, reps = 8, passes = 4;
+    // trial steps k0 .. k0+reps stay inside [1, nt-2] (records are read at step q+1)
+    if (nt < 4 * reps) return TOMO_OK;   // short sweeps keep the defaults
+    const int k0 = nt / 2 - reps;
     float best_f = 1e30f, best_a = 1e30f;
     // forward: rows per warp; adjoint: rows per warp x register/unroll variant
     for (int rows : cands) {
         if (rows > 4 * c->geo.ny) continue;
         for (int which = 0; which < 5; ++which) {
-            float ms = 0.f;
-            for (int pass = 0; pass < 2; ++pass) {   // first pass warms up
+            float ms = 1e30f;
+            for (int pass = 0; pass < passes; ++pass) {   // first pass warms up
                 CU(c, cudaEventRecord(c->ev0, c->st));
                 for (int t = 0; t < reps; ++t) {
                     if (which == 0) launch_fwd_strip(rows, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), c->st);
@@ -209,40 +252,49 @@ tomo_status autotune(tomo_ctx* c) {
                 }
                 CU(c, cudaEventRecord(c->ev1, c->st));
                 CU(c, cudaEventSynchronize(c->ev1));
-                CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+                float t_ms = 0.f;
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) ms = std::min(ms, t_ms);
             }
-            if (which == 0 && ms < best_f) { best_f = ms; c->rows_fwd = rows; }
-            if (which > 0 && ms < best_a) { best_a = ms; c->rows_adj = rows; c->adj_variant = which - 1; }
+            if (which == 0 && ms < best_f) { best_f = ms; c->rows_fwd = rows; c->fwd_pair = false; }
+            if (which > 0 && ms < best_a) {
+                best_a = ms; c->rows_adj = rows; c->adj_variant = which - 1; c->adj_pair = false;
+            }
         }
         for (int code : {rows, 100 + rows}) {   // two forward steps per launch, 2 or 4 cells per lane
             if (rows < 4 || c->S < 4) break;
-            float ms = 0.f;
-            for (int pass = 0; pass < 2; ++pass) {
+            float ms = 1e30f;
+            for (int pass = 0; pass < passes; ++pass) {
                 CU(c, cudaEventRecord(c->ev0, c->st));
                 for (int t = 0; t < reps; t += 2)
                     launch_fwd2_strip(code, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), fwd_args(c, k0 + t + 1, 0, ng),
                                       false, false, c->st);
                 CU(c, cudaEventRecord(c->ev1, c->st));
                 CU(c, cudaEventSynchronize(c->ev1));
-                CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+                float t_ms = 0.f;
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) ms = std::min(ms, t_ms);
             }
             if (ms < best_f) { best_f = ms; c->rows_fwd2 = code; c->fwd_pair = true; }
         }
         if (rows >= 4) {   // two steps per launch: reps/2 launches cover the same steps
-            float ms = 0.f;
-            for (int pass = 0; pass < 2; ++pass) {
+            float ms = 1e30f;
+            for (int pass = 0; pass < passes; ++pass) {
                 CU(c, cudaEventRecord(c->ev0, c->st));
                 for (int t = 0; t < reps; t += 2)
                     launch_adj2_strip(rows, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, ng),
                                       adj_args(c, k0 + reps - t - 1, 0, ng), c->st);
                 CU(c, cudaEventRecord(c->ev1, c->st));
                 CU(c, cudaEventSynchronize(c->ev1));
-                CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+                float t_ms = 0.f;
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) ms = std::min(ms, t_ms);
             }
             if (ms < best_a) { best_a = ms; c->rows_adj2 = rows; c->adj_pair = true; }
         }
     }
     CU(c, cudaGetLastError());
+    if (cache && *cache) tune_cache_append(c, cache);
     return TOMO_OK;
 }
 
@@ -720,6 +772,8 @@ tomo_status ensure_learned_buffers(tomo_ctx* c) {
     TRY(c->alloc(&c->fsave, N, "saved field"));
     TRY(c->alloc(&c->dnet, N, "network update"));
     TRY(c->alloc(&c->illum_max, 1, "illumination max"));
+    TRY(c->alloc(&c->dsave, N, "saved direction"));
+    TRY(c->alloc(&c->maxsave, 1, "saved direction max"));
     return TOMO_OK;
 }
 
@@ -1051,6 +1105,63 @@ tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule
         stats->cell_updates = 3.0 * (double)g.G * (double)(g.nt - 2) * (double)N;
         stats->kernel_launches = (double)(c->launches - launches0);
     }
+    return TOMO_OK;
+}
+
+tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fallback, float* d_f,
+                             const float* d_f_true, double target_epsilon, int32_t max_iters, int32_t window,
+                             double* eps_log, int32_t* accepted_log, int32_t* iters_done, double* seconds) {
+    if (!c || !net || !fallback || !d_f || max_iters < 0 || window < 1 || window > 64)
+        return c ? c->fail(TOMO_ERR_ARG, "bad tomo_run_learned arguments") : TOMO_ERR_ARG;
+    if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
+    CU(c, cudaSetDevice(c->dev));
+    const Geometry& g = c->geo;
+    const int64_t N = g.N;
+    const size_t fb = sizeof(float) * N;
+    TRY(ensure_learned_buffers(c));
+    CU(c, cudaMemcpyAsync(c->f, d_f, fb, cudaMemcpyDeviceToDevice, c->st));
+    if (d_f_true) CU(c, cudaMemcpyAsync(c->ftrue, d_f_true, fb, cudaMemcpyDeviceToDevice, c->st));
+    TRY(compute_illumination(c));
+    const auto t0 = std::chrono::steady_clock::now();
+    double r0 = 0.0, r1 = 0.0;
+    TRY(features_core(c, &r0));            // gradient, direction and features at the start field
+    std::vector<double> hist(1, r0);       // residuals of the last `window` fields
+    int done = 0;
+    for (int it = 0; it < max_iters; ++it) {
+        const double s = sched_scale(fallback, it);
+        if (!std::isfinite(s)) return c->fail(TOMO_ERR_ARG, "bad schedule");
+        tomo_status ns = net_infer(net, c->feat, g.ny, g.nx, c->dnet, c->st);
+        if (ns != TOMO_OK) return c->fail(ns, "network: %s", tomo_net_last_error(net));
+        CU(c, cudaMemcpyAsync(c->fsave, c->f, fb, cudaMemcpyDeviceToDevice, c->st));
+        CU(c, cudaMemcpyAsync(c->dsave, c->dir, fb, cudaMemcpyDeviceToDevice, c->st));
+        CU(c, cudaMemcpyAsync(c->maxsave, c->maxabs, sizeof(unsigned int), cudaMemcpyDeviceToDevice, c->st));
+        launch_apply(c->f, c->dnet, c->mask, N, 1.0, nullptr, c->st);
+        c->launches += 7;
+        // the check is the gradient sweep of the proposal: accepted, it is the next step's gradient
+        TRY(features_core(c, &r1));
+        const bool ok = r1 < *std::max_element(hist.begin(), hist.end());
+        if (ok) {
+            r0 = r1;
+        } else {
+            CU(c, cudaMemcpyAsync(c->f, c->fsave, fb, cudaMemcpyDeviceToDevice, c->st));
+            launch_apply(c->f, c->dsave, c->mask, N, s, fallback->normalize ? c->maxsave : nullptr, c->st);
+            ++c->launches;
+            TRY(features_core(c, &r0));
+        }
+        hist.push_back(r0);
+        if ((int)hist.size() > window) hist.erase(hist.begin());
+        double eps = std::numeric_limits<double>::quiet_NaN();
+        if (d_f_true) TRY(epsilon(c, &eps));
+        if (eps_log) eps_log[it] = eps;
+        if (accepted_log) accepted_log[it] = ok ? 1 : 0;
+        done = it + 1;
+        if (d_f_true && eps <= target_epsilon) break;
+    }
+    CU(c, cudaMemcpyAsync(d_f, c->f, fb, cudaMemcpyDeviceToDevice, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    CU(c, cudaGetLastError());
+    if (iters_done) *iters_done = done;
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return TOMO_OK;
 }
 

@@ -336,12 +336,22 @@ __global__ void k_avgw_apply(const float* __restrict__ corr, int G, int64_t N, f
     }
 }
 
-__global__ void k_sum_parts(const double* __restrict__ part, int rows, int nb, double* __restrict__ out) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= rows) return;
+// One block per row: strided per-thread sums, then a fixed-shape tree, so the
+// order of the additions depends only on (nb, SUM_THREADS).
+constexpr int SUM_THREADS = 256;
+__global__ void __launch_bounds__(SUM_THREADS) k_sum_parts(const double* __restrict__ part, int nb,
+                                                          double* __restrict__ out) {
+    __shared__ double sh[SUM_THREADS];
+    const double* p = part + (int64_t)blockIdx.x * nb;
     double acc = 0.0;
-    for (int b = 0; b < nb; ++b) acc += part[(int64_t)r * nb + b];
-    out[r] = acc;
+    for (int b = threadIdx.x; b < nb; b += SUM_THREADS) acc += p[b];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = SUM_THREADS / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
 }
 
 __global__ void k_maxabs(const float* __restrict__ dir, const uint8_t* __restrict__ mask, int64_t N,
@@ -480,7 +490,7 @@ void launch_avgw_apply(const float* corr, int G, int64_t N, float* f, const uint
 }
 
 void launch_sum_parts(const double* part, int rows, int nb, double* out, void* st) {
-    k_sum_parts<<<(rows + 127) / 128, 128, 0, S(st)>>>(part, rows, nb, out);
+    if (rows > 0) k_sum_parts<<<rows, SUM_THREADS, 0, S(st)>>>(part, nb, out);
 }
 
 void launch_maxabs(const float* dir, const uint8_t* mask, int64_t N, unsigned int* out, void* st) {

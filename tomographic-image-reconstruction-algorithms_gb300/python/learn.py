@@ -13,8 +13,9 @@ Pipeline, all compute in libtomo.so's kernels (torch only holds device buffers):
   2. training: Adam on the masked mean squared error, on the GPU.
   3. evaluation (time to image): on the 512x512 workload, plain weighted SIRT
      runs `plain_iters` iterations; the learned iteration (network proposal
-     accepted only when the record residual drops, else the plain step) runs
-     until it reaches the plain method's final image error.
+     accepted only when the record residual drops, else the plain step; see
+     tomo_run_learned) runs until it reaches the plain method's final image
+     error.
 
 Usage:  python learn.py [--phantoms 1000] [--iters 20] [--epochs 8] [--out weights.bin]
 """
@@ -49,15 +50,19 @@ def phantom(cfg, seed, rmin, rmax):
     return tomo.phantom_cfg(cfg.nx, cfg.ny, 1, 8, rmin, rmax, 0.15, 0.01, 0.8 * cfg.radius, seed)
 
 
+TRAIN_RADII = (8.0, 45.0)   # ellipse semi-axes of the training phantoms (cells)
+
+
 def mask_of(cfg):
     y, x = np.mgrid[0:cfg.ny, 0:cfg.nx]
     r = cfg.radius - 1.5
     return (((x - 0.5 * cfg.nx) ** 2 + (y - 0.5 * cfg.ny) ** 2) < r * r).astype(np.float32)
 
 
-def generate(n_phantoms, iters, lookahead=6, seed0=4000, device=0, log=print):
+def generate(n_phantoms, iters, lookahead=6, seed0=4000, device=0, target="lookahead", log=print):
     """Plain weighted SIRT trajectories -> (features [M,3,H,W], targets [M,H,W], mask [H,W]) on the GPU,
-    M = n_phantoms * (iters - lookahead + 1)."""
+    M = n_phantoms * (iters - lookahead + 1).  target "lookahead": f_{t+K} - f_t; "truth":
+    mask * (f_true - f_t), the update that would complete the image."""
     import torch
 
     dev = torch.device("cuda", device)
@@ -73,15 +78,19 @@ def generate(n_phantoms, iters, lookahead=6, seed0=4000, device=0, log=print):
     j = 0
     with tomo.Context(cfg) as ctx:
         for ph in range(n_phantoms):
-            fo = phantom(cfg, seed0 + ph, 5.0, 30.0)
+            fo = phantom(cfg, seed0 + ph, *TRAIN_RADII)
             ctx.set_records(ctx.generate_data(fo, noise_level=0.01, seed=seed0 + ph))
+            d_fo = torch.from_numpy(fo).to(dev)
             traj[0].zero_()
             for it in range(iters):
                 torch.cuda.synchronize(dev)   # torch writes the trajectory on its own stream
                 ctx.features_device(traj[it].data_ptr(), feat_t[it].data_ptr())
                 traj[it + 1] = traj[it] + STEP * m * feat_t[it, 1]      # the plain weighted SIRT step
             feats[j:j + per] = feat_t[:per]
-            tgts[j:j + per] = traj[lookahead:lookahead + per] - traj[:per]
+            if target == "truth":
+                tgts[j:j + per] = m * (d_fo - traj[:per])
+            else:
+                tgts[j:j + per] = traj[lookahead:lookahead + per] - traj[:per]
             j += per
             if ph % 100 == 0:
                 log(f"  data: phantom {ph}/{n_phantoms}, {time.time() - t0:.1f} s")
@@ -89,9 +98,34 @@ def generate(n_phantoms, iters, lookahead=6, seed0=4000, device=0, log=print):
     return feats, tgts, m, time.time() - t0
 
 
-def train(net, feats, tgts, mask, epochs, batch=16, lr=1e-3, seed=0, log=print):
+def masked_mse(out, tgts, mask):
+    """Mean over samples of sum(mask*(out-t)^2)/sum(mask)."""
+    return float(((out - tgts) ** 2 * mask).sum() / (mask.sum() * out.shape[0]))
+
+
+def baselines(feats, tgts, mask, lookahead):
+    """Losses of two fixed predictors: zero, and lookahead plain steps along the current direction."""
+    return {"zero": masked_mse(0 * tgts, tgts, mask),
+            "linear": masked_mse(lookahead * STEP * feats[:, 1] * mask, tgts, mask)}
+
+
+def evaluate(net, feats, tgts, mask, batch=16):
     import torch
 
+    M, _, H, W = feats.shape
+    out = torch.empty((batch, H, W), dtype=torch.float32, device=feats.device)
+    acc, n = 0.0, 0
+    for b in range(0, M - batch + 1, batch):
+        fb = feats[b:b + batch].contiguous()
+        torch.cuda.synchronize(feats.device)
+        net.forward_device(fb.data_ptr(), batch, H, W, out.data_ptr())
+        torch.cuda.synchronize(feats.device)
+        acc += masked_mse(out, tgts[b:b + batch], mask) * batch
+        n += batch
+    return acc / max(n, 1)
+
+
+def train(net, feats, tgts, mask, epochs, batch=16, lr=1e-3, seed=0, log=print):
     M, _, H, W = feats.shape
     bm = mask.expand(batch, H, W).contiguous()
     rng = np.random.default_rng(seed)
@@ -99,6 +133,8 @@ def train(net, feats, tgts, mask, epochs, batch=16, lr=1e-3, seed=0, log=print):
     t0 = time.time()
     s = 0
     losses = []
+    import torch
+
     for ep in range(epochs):
         perm = torch.from_numpy(rng.permutation(M)).to(feats.device)
         acc = 0.0
@@ -115,7 +151,7 @@ def train(net, feats, tgts, mask, epochs, batch=16, lr=1e-3, seed=0, log=print):
     return losses, time.time() - t0
 
 
-def time_to_image(net, plain_iters=30, seed=2001, device=0, log=print):
+def time_to_image(net, plain_iters=30, seed=2001, device=0, windows=(1, 2), log=print):
     """Plain weighted SIRT for plain_iters iterations vs the learned iteration to the same image error."""
     import torch
 
@@ -144,32 +180,32 @@ def time_to_image(net, plain_iters=30, seed=2001, device=0, log=print):
         log(f"  plain: {plain_iters} iterations, eps {eps[0]:.3f} -> {target:.3f} %, {t_plain:.3f} s")
         d_f.zero_()
         torch.cuda.synchronize(dev)
-        ctx.iterate_learned(net, sched, 0, d_f.data_ptr(), d_fo.data_ptr())   # warm up (illumination, graphs)
-        d_f.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        leps, accepted = [], 0
-        for it in range(3 * plain_iters):
-            st, acc = ctx.iterate_learned(net, sched, it, d_f.data_ptr(), d_fo.data_ptr())
-            leps.append(st.epsilon)
-            accepted += int(acc)
-            if st.epsilon <= target:
-                break
-        ctx.synchronize()
-        t_learned = time.perf_counter() - t0
-        log(f"  learned: {len(leps)} iterations ({accepted} accepted), eps -> {leps[-1]:.3f} %, {t_learned:.3f} s")
+        ctx.run_learned(net, sched, d_f.data_ptr(), d_fo.data_ptr(), -1.0, 1)   # warm up (illumination, graphs)
         out = {"plain_iters": plain_iters, "plain_seconds": t_plain, "plain_final_epsilon": target,
-               "plain_epsilon": eps, "learned_iters": len(leps), "learned_accepted": accepted,
-               "learned_seconds": t_learned, "learned_final_epsilon": leps[-1], "learned_epsilon": leps,
-               "reached": leps[-1] <= target, "speedup": t_plain / t_learned if leps[-1] <= target else None}
+               "plain_epsilon": eps, "learned": {}}
+        for win in windows:
+            d_f.zero_()
+            torch.cuda.synchronize(dev)
+            leps, acc, t_learned = ctx.run_learned(net, sched, d_f.data_ptr(), d_fo.data_ptr(), target,
+                                                   3 * plain_iters, win)
+            leps = [float(e) for e in leps]
+            reached = bool(leps[-1] <= target)
+            log(f"  learned (window {win}): {len(leps)} iterations ({int(acc.sum())} accepted), "
+                f"eps -> {leps[-1]:.3f} %, {t_learned:.3f} s, speedup "
+                f"{t_plain / t_learned if reached else float('nan'):.2f}")
+            out["learned"][str(win)] = {
+                "iters": len(leps), "accepted": [int(a) for a in acc], "seconds": t_learned,
+                "final_epsilon": leps[-1], "epsilon": leps, "reached": reached,
+                "speedup": t_plain / t_learned if reached else None}
     return out
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--phantoms", type=int, default=1000)
-    ap.add_argument("--iters", type=int, default=26)
+    ap.add_argument("--iters", type=int, default=36)
     ap.add_argument("--lookahead", type=int, default=6)
+    ap.add_argument("--target", default="lookahead", choices=["lookahead", "truth"])
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
@@ -179,19 +215,27 @@ def main():
     net = tomo.Net(0, seed=7)
     report = {}
     if not args.eval_only:
-        feats, tgts, m, t_data = generate(args.phantoms, args.iters, args.lookahead)
+        feats, tgts, m, t_data = generate(args.phantoms, args.iters, args.lookahead, target=args.target)
+        report["target"] = args.target
         report["lookahead"] = args.lookahead
         report["pairs"] = int(feats.shape[0])
         report["data_seconds"] = t_data
+        nval = max(16, int(0.05 * feats.shape[0]) // 16 * 16)      # held out: the last phantoms
+        fv, tv = feats[-nval:], tgts[-nval:]
+        feats, tgts = feats[:-nval], tgts[:-nval]
+        report["baseline_loss"] = baselines(fv, tv, m, args.lookahead)
+        print(f"  held-out baselines: {report['baseline_loss']}")
         losses, t_train = train(net, feats, tgts, m, args.epochs, args.batch, args.lr)
         report["losses"] = losses
         report["train_seconds"] = t_train
+        report["val_loss"] = evaluate(net, fv, tv, m)
+        print(f"  held-out loss {report['val_loss']:.3e}")
         os.makedirs(os.path.dirname(args.out), exist_ok=True)
         net.save(args.out)
-        del feats, tgts
+        del feats, tgts, fv, tv
     else:
         net.load(args.out)
-    report["time_to_image"] = time_to_image(net)
+    report["time_to_image"] = time_to_image(net, windows=(1,))
     print(json.dumps(report))
 
 

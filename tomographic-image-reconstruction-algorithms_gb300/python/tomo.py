@@ -173,6 +173,8 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_net_train_step_device": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, DP]),
         "tomo_features_device": (i32, [vp, vp, vp, DP]),
         "tomo_iterate_learned": (i32, [vp, vp, C.POINTER(Schedule), i32, vp, vp, C.POINTER(IterStats), IP]),
+        "tomo_run_learned": (i32, [vp, vp, C.POINTER(Schedule), vp, vp, C.c_double, i32, i32, DP, IP, IP,
+                                   C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -332,6 +334,19 @@ class Context:
         self._check(lib().tomo_iterate_learned(self.h, net.h, C.byref(fallback), it, C.c_void_p(d_f),
                                                C.c_void_p(d_ftrue or None), C.byref(stats), C.byref(acc)))
         return stats, bool(acc.value)
+
+    def run_learned(self, net: "Net", fallback: Schedule, d_f: int, d_ftrue: int = 0,
+                    target_eps: float = -1.0, max_iters: int = 50, window: int = 1):
+        """Learned iterations on d_f until epsilon <= target_eps or max_iters:
+        (epsilon per iteration, accepted per iteration, wall seconds)."""
+        eps = np.full(max(max_iters, 1), np.nan)
+        acc = np.zeros(max(max_iters, 1), np.int32)
+        done, secs = C.c_int32(), C.c_double()
+        self._check(lib().tomo_run_learned(self.h, net.h, C.byref(fallback), C.c_void_p(d_f),
+                                           C.c_void_p(d_ftrue or None), target_eps, max_iters, window, _dp(eps),
+                                           _ip(acc), C.byref(done), C.byref(secs)))
+        n = done.value
+        return eps[:n], acc[:n].astype(bool), secs.value
 
     @property
     def stream(self) -> int:
