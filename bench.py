@@ -11,9 +11,13 @@ fused correlation, checkpoint recompute, and the update.
 
 metric: stencil GB/s, algorithmic bytes per iteration = G*nx*ny*(nt-2)*(16+20)
 (16 B per forward and 20 B per adjoint cell-update; recompute not credited).
+On c2 the line also carries time_to_image: wall time of 30 plain weighted SIRT
+iterations from f = 0 against the learned update (the shipped network in
+weights/learned_update.bin, residual-checked) run until it reaches the same
+image error, with the speed-up and the gradient sweeps each used.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl tomo|reference]
-                    [--workload c2|c1|ref192|c5]
+                    [--workload c2|c1|c3|ref192|c5] [--no-cpu] [--no-learned]
 Under torchrun each rank reconstructs its own independent phantom on its own
 GPU (weak scaling over independent reconstructions, no collective on the
 data path); rank 0 prints one JSON line.
@@ -59,6 +63,94 @@ WORKLOADS = {
                    cfg=None, phantom=None, noise=0.0, method=tomo.SIRT_NORM,
                    sched=dict(kind=tomo.SCHED_POWER, omega=1e5, alpha=0.5, beta=0.5, gamma=1.0)),
 }
+
+
+C3_SIZES = (128, 192, 256, 384, 512)
+
+
+def c3_configs(device, n=64):
+    """The batched workload: n phantoms cycling through the grid sizes N, N/2 transducers on a
+    radius-0.43N circle in groups of 8, nt = 10 N, checkpoint interval about sqrt(2 nt)."""
+    out = []
+    for i in range(n):
+        N = C3_SIZES[i % len(C3_SIZES)]
+        nt = 10 * N
+        out.append(tomo.cfg_config(nx=N, ny=N, nt=nt, n_transducers=N // 2, group_size=8, radius=0.43 * N,
+                                   ckpt_interval=int(round((2 * nt) ** 0.5)), device=device))
+    return out
+
+
+def run_batch(args, local, rank, world, dist):
+    """c3: 64 independent reconstructions of uneven sizes advanced together (tomo_iterate_batch)."""
+    import torch
+
+    dev = torch.device("cuda", local)
+    cfgs = c3_configs(local)
+    ctxs, d_fs, d_fts, recs, fos = [], [], [], [], []
+    for i, cfg in enumerate(cfgs):
+        N = cfg.nx
+        fo = tomo.phantom_cfg(N, N, 1, 8, N / 50.0, N / 8.5, 0.15, 0.01, 0.8 * cfg.radius, 5000 + i + 1000 * rank)
+        ctx = tomo.Context(cfg)
+        rec = ctx.generate_data(fo, noise_level=0.01, seed=5000 + i)
+        ctx.set_records(rec)
+        ctxs.append(ctx)
+        fos.append(fo)
+        recs.append(torch.from_numpy(rec).pin_memory())
+        d_fs.append(torch.zeros(fo.shape, dtype=torch.float32, device=dev))
+        d_fts.append(torch.from_numpy(fo).to(dev))
+    torch.cuda.synchronize(dev)
+    sched = tomo.schedule(omega=0.02, normalize=1)
+    bytes_it = sum(algorithmic_bytes(c, tomo.n_groups(c)) for c in cfgs)
+    ptrs = [t.data_ptr() for t in d_fs]
+    tptrs = [t.data_ptr() for t in d_fts]
+    tomo.iterate_batch(ctxs, tomo.SIRT_NORM, sched, 0, args.warmup, ptrs, tptrs)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        eps, secs = tomo.iterate_batch(ctxs, tomo.SIRT_NORM, sched, args.warmup, args.steps, ptrs, tptrs)
+    clocks = clk.summary()
+    t_max = secs
+    if dist:
+        t = torch.tensor([secs], dtype=torch.float64, device=dev if dist.get_backend() == "nccl" else "cpu")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * bytes_it * args.steps / t_max / 1e9
+    # end to end: every step copies each phantom's records and field in from pinned host memory and
+    # the field back out
+    f_host = [torch.zeros(fo.shape, dtype=torch.float32).pin_memory() for fo in fos]
+    t0 = time.perf_counter()
+    for s_ in range(args.steps):
+        for i, ctx in enumerate(ctxs):
+            ctx.set_records(recs[i].numpy())
+            d_fs[i].copy_(f_host[i], non_blocking=True)
+        torch.cuda.synchronize(dev)
+        tomo.iterate_batch(ctxs, tomo.SIRT_NORM, sched, args.warmup + args.steps + s_, 1, ptrs, tptrs)
+        for i in range(len(ctxs)):
+            f_host[i].copy_(d_fs[i], non_blocking=True)
+        torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    h2d = sum(4 * (fo.size + r.numel()) for fo, r in zip(fos, recs))
+    if rank == 0:
+        line = {
+            "metric": metric_name(), "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded ellipse phantoms + smoothed noise, 1% Gaussian record noise)",
+            "config": {"workload": "c3: 64 phantoms of N in {128,192,256,384,512} cycling, N/2 transducers "
+                                   "r=0.43N, groups of 8, nt 10N, checkpoint ~sqrt(2 nt), plain weighted SIRT, "
+                                   "all phantoms advanced together (tomo_iterate_batch)",
+                       "phantoms": len(cfgs), "l2": "inputs larger than L2",
+                       "parallelism": f"replicas{world}" if world > 1 else "single GPU"},
+            "phantom_iter_per_s": world * len(cfgs) * args.steps / t_max,
+            "epsilon_last_mean": float(np.nanmean(eps[:, -1])),
+            "e2e": {"value": world * bytes_it * args.steps / e2e_s / 1e9, "unit": "GB/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": sum(4 * fo.size for fo in fos)},
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    for c in ctxs:
+        c.close()
 
 
 def make_config(w, device):
@@ -161,7 +253,11 @@ def cpu_sample(w, cfg, fo, rec, target_s=12.0):
 def reference_arm(args, w, rank, world):
     if rank != 0:
         return
-    cfg = make_config(w, 0)
+    if w is None:   # c3: the sweep of its largest phantom stands for the batch
+        cfg = c3_configs(0)[C3_SIZES.index(512)]
+        w = {"desc": "largest c3 phantom (512x512, nt 5120, 256 transducers, 32 groups of 8)"}
+    else:
+        cfg = make_config(w, 0)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle_lib as O
 
@@ -199,6 +295,39 @@ def metric_name():
     return "stencil GB/s (algorithmic 36 B per forward+adjoint cell-update) of one plain weighted SIRT iteration"
 
 
+WEIGHTS = os.path.join(PKG, "weights", "learned_update.bin")
+
+
+def time_to_image(ctx, w, sched, d_f, d_ft, torch, dev, plain_iters=30):
+    """Wall time of plain weighted SIRT for plain_iters iterations from f = 0 against the learned
+    update (shipped network, residual-checked, fused run loop) to the same image error."""
+    if not os.path.exists(WEIGHTS):
+        return {"unavailable": "no trained weights at " + os.path.relpath(WEIGHTS, REPO)}
+    net = tomo.Net(dev.index or 0)
+    net.load(WEIGHTS)
+    d_f.zero_()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    eps = [ctx.iterate_device(w["method"], sched, it, d_f.data_ptr(), 0, d_ft.data_ptr()).epsilon
+           for it in range(plain_iters)]
+    ctx.synchronize()
+    t_plain = time.perf_counter() - t0
+    d_f.zero_()
+    torch.cuda.synchronize(dev)
+    ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), -1.0, 1)    # warm-up: illumination, graphs
+    d_f.zero_()
+    torch.cuda.synchronize(dev)
+    leps, acc, t_learned = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), eps[-1], 3 * plain_iters)
+    net.close()
+    reached = bool(leps[-1] <= eps[-1])
+    n_acc = int(acc.sum())
+    return {"plain_seconds": t_plain, "plain_iters": plain_iters, "target_epsilon": eps[-1],
+            "learned_seconds": t_learned, "learned_iters": len(leps), "learned_accepted": n_acc,
+            "learned_epsilon": float(leps[-1]), "reached": reached,
+            "gradient_sweeps": {"plain": plain_iters, "learned": 1 + len(leps) + (len(leps) - n_acc)},
+            "speedup": t_plain / t_learned if reached else None}
+
+
 def read_tuning(path):
     """The strip-kernel choice of the autotuner, from its cache file (last line)."""
     try:
@@ -218,12 +347,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tomo", choices=["tomo", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-learned", action="store_true", help="skip the time-to-image leg (c2)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    w = WORKLOADS[args.workload]
+    w = WORKLOADS.get(args.workload)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -249,6 +379,11 @@ def main():
     if not torch.cuda.is_available():
         raise SystemExit("bench.py needs a CUDA GPU (libtomo.so has no CPU path)")
     tomo.lib()
+    if args.workload == "c3":
+        run_batch(args, local, rank, world, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
     cfg = make_config(w, local)
     fo = make_phantom(w, cfg, 2001 + 1000 * rank)
 
@@ -330,6 +465,8 @@ def main():
     h2d = 4 * (fo.size * 2 + rec.size)
     d2h = 4 * fo.size + 8
 
+    tti = time_to_image(ctx, w, sched, d_f, d_ft, torch, dev) if args.workload == "c2" and not args.no_learned else None
+
     # roofline of the dominant kernel, timed live on the context stream
     info = ctx.info
     nt, K, nseg = cfg.nt, info.ckpt_interval, info.n_segments
@@ -373,6 +510,8 @@ def main():
                                    "adjoint_step_GBps": adj_b / (adj_ms * 1e-3) / 1e9}},
             "clocks": clocks,
         }
+        if tti is not None:
+            line["time_to_image"] = tti
         if cpu:
             line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         print(json.dumps(line), flush=True)

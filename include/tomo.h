@@ -270,6 +270,20 @@ tomo_status tomo_run_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedule* 
                              const float* d_f_true, double target_epsilon, int32_t max_iters, int32_t window,
                              double* eps_log, int32_t* accepted_log, int32_t* iters_done, double* seconds);
 
+/* Several independent reconstructions advanced together (the batched
+ * many-phantom workload: phantoms of different grid sizes, each its own
+ * context and stream).  Context i runs `iters` iterations of `method` from
+ * iteration index iter0 on its device field d_f[i] (records set beforehand),
+ * one host thread per context, so the contexts' kernels overlap on the GPU.
+ * d_f_true (optional, per context) fills eps_log[i * iters + it] (optional).
+ * *seconds (optional) is the wall time of the whole batch.  Returns the first
+ * failing context's status (its tomo_last_error has the reason).  Replaces
+ * running the reference drivers one after another; the reference has no batch
+ * entry point. */
+tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const tomo_schedule* sched,
+                               int32_t iter0, int32_t iters, float** d_f, const float** d_f_true, double* eps_log,
+                               double* seconds);
+
 /* Forward solve without any device allocation (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc: applications whose own
  * pool allocator owns all device memory, or latency-bound loops where

@@ -171,3 +171,34 @@ def test_run_learned_stops_at_target(torch_dev):
         with pytest.raises(tomo.TomoError):
             ctx.run_learned(net, tomo.schedule(omega=0.02, normalize=1), d_f.data_ptr(), d_ft.data_ptr(),
                             1e-2, 10, window=0)
+
+
+def test_shipped_network_gain(torch_dev):
+    """What the trained network gains on the 512x512 / 256-transducer workload: the learned
+    update reaches the image error of 30 plain weighted-SIRT iterations with at most half the
+    gradient sweeps (each sweep is one forward plus one adjoint solve of all 32 groups)."""
+    import os
+
+    torch, dev = torch_dev
+    weights = os.path.join(tomo.PKG_DIR, "weights", "learned_update.bin")
+    assert os.path.exists(weights), "trained weights are part of the package"
+    cfg = tomo.cfg_config(nx=512, ny=512, nt=2500, n_transducers=256, group_size=8, radius=220.0,
+                          ckpt_interval=50)
+    fo = tomo.phantom_cfg(512, 512, 1, 8, 10.0, 60.0, 0.15, 0.01, 176.0, 2001)
+    sched = tomo.schedule(omega=0.02, normalize=1)
+    with tomo.Context(cfg) as ctx:
+        ctx.set_records(ctx.generate_data(fo, noise_level=0.01, seed=77))
+        d_f = torch.zeros(fo.shape, dtype=torch.float32, device=dev)
+        d_ft = torch.from_numpy(fo).to(dev)
+        torch.cuda.synchronize(dev)
+        for it in range(30):
+            st = ctx.iterate_device(tomo.SIRT_NORM, sched, it, d_f.data_ptr(), 0, d_ft.data_ptr())
+        target = st.epsilon
+        net = tomo.Net(0)
+        net.load(weights)
+        d_f.zero_()
+        torch.cuda.synchronize(dev)
+        eps, acc, _ = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), target, 30)
+        sweeps = 1 + len(eps) + int((~acc).sum())
+        assert eps[-1] <= target, (list(eps), target)
+        assert sweeps <= 15, (sweeps, list(eps), list(acc))

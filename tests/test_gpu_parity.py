@@ -245,11 +245,13 @@ def test_two_step_kernels_match_one_step(nt, monkeypatch):
     meas = O.forward(cfg0, fo.astype(np.float64))
     f0 = blob_phantom(64, 72, seed=9, amp=0.01)
     outs = []
-    for pair, fwd_rows in (("0", "4"), ("1", "4"), ("1", "104")):   # 104: four cells per lane
+    # fwd 104: four cells per lane; adj 104: correlation read one row ahead
+    for pair, fwd_rows, adj_rows in (("0", "4", "4"), ("1", "4", "4"), ("1", "104", "104")):
         monkeypatch.setenv("TOMO_STRIP_ROWS", "4")
         monkeypatch.setenv("TOMO_FWD_PAIR", pair)
         monkeypatch.setenv("TOMO_FWD_PAIR_ROWS", fwd_rows)
         monkeypatch.setenv("TOMO_ADJ_PAIR", pair)
+        monkeypatch.setenv("TOMO_ADJ_PAIR_ROWS", adj_rows)
         with tomo.Context(small_cfg(nt=nt, ckpt_interval=9)) as ctx:
             rec = ctx.forward(fo)
             dfg, _, r2 = ctx.gradient(f0, meas)

@@ -27,6 +27,7 @@
 #include <map>
 #include <string>
 #include <tuple>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -57,6 +58,8 @@ struct tomo_ctx {
     double *rpart = nullptr, *part = nullptr, *sums = nullptr;
     unsigned int* maxabs = nullptr;
     int32_t *box = nullptr, *emit = nullptr, *rcv = nullptr, *rid = nullptr;
+    uint32_t* rbits = nullptr;
+    int rwords = 0;
     float* src = nullptr;
     uint8_t* mask = nullptr;
     int64_t bytes = 0;
@@ -228,6 +231,7 @@ tomo_status autotune(tomo_ctx* c) {
         c->rows_fwd = c->rows_adj = c->rows_adj2 = std::atoi(e);
         if (const char* v = std::getenv("TOMO_ADJ_VARIANT")) c->adj_variant = std::atoi(v);
         if (const char* v = std::getenv("TOMO_ADJ_PAIR")) c->adj_pair = std::atoi(v) != 0;
+        if (const char* v = std::getenv("TOMO_ADJ_PAIR_ROWS")) c->rows_adj2 = std::atoi(v);
         if (const char* v = std::getenv("TOMO_FWD_PAIR")) c->fwd_pair = std::atoi(v) != 0 && c->S >= 4;
         c->rows_fwd2 = c->rows_fwd;
         if (const char* v = std::getenv("TOMO_FWD_PAIR_ROWS")) c->rows_fwd2 = std::atoi(v);
@@ -277,12 +281,13 @@ tomo_status autotune(tomo_ctx* c) {
             }
             if (ms < best_f) { best_f = ms; c->rows_fwd2 = code; c->fwd_pair = true; }
         }
-        if (rows >= 4) {   // two steps per launch: reps/2 launches cover the same steps
+        for (int code : {rows, 100 + rows}) {   // two steps per launch: reps/2 launches cover the same steps
+            if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {
                 CU(c, cudaEventRecord(c->ev0, c->st));
                 for (int t = 0; t < reps; t += 2)
-                    launch_adj2_strip(rows, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, ng),
+                    launch_adj2_strip(code, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, ng),
                                       adj_args(c, k0 + reps - t - 1, 0, ng), c->st);
                 CU(c, cudaEventRecord(c->ev1, c->st));
                 CU(c, cudaEventSynchronize(c->ev1));
@@ -290,7 +295,7 @@ tomo_status autotune(tomo_ctx* c) {
                 CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
                 if (pass > 0) ms = std::min(ms, t_ms);
             }
-            if (ms < best_a) { best_a = ms; c->rows_adj2 = rows; c->adj_pair = true; }
+            if (ms < best_a) { best_a = ms; c->rows_adj2 = code; c->adj_pair = true; }
         }
     }
     CU(c, cudaGetLastError());
@@ -369,6 +374,8 @@ tomo_status create_buffers(tomo_ctx* c) {
     else {
         TRY(c->alloc(&c->emit, G * g.gs, "emitters"));
         TRY(c->alloc(&c->rid, N, "receiver map"));
+        c->rwords = ((g.nx + 31) / 32 + 31) / 32;
+        TRY(c->alloc(&c->rbits, (int64_t)g.ny * c->rwords, "receiver row bitmap"));
     }
     CU(c, cudaMemsetAsync(c->rr, 0, sizeof(float) * P * nt * nch, c->st));
     CU(c, cudaMemsetAsync(c->meas, 0, sizeof(float) * G * nt * nch, c->st));
@@ -381,13 +388,22 @@ tomo_status create_buffers(tomo_ctx* c) {
     else {
         CU(c, cudaMemcpyAsync(c->emit, g.emit.data(), sizeof(int32_t) * G * g.gs, cudaMemcpyHostToDevice, c->st));
         CU(c, cudaMemcpyAsync(c->rid, g.rid.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, c->st));
+        std::vector<uint32_t> bits((size_t)g.ny * c->rwords, 0u);
+        for (int64_t q = 0; q < N; ++q)
+            if (g.rid[q] >= 0) {
+                const int b = (int)(q % g.nx) >> 5;
+                bits[(size_t)(q / g.nx) * c->rwords + (b >> 5)] |= 1u << (b & 31);
+            }
+        CU(c, cudaMemcpyAsync(c->rbits, bits.data(), sizeof(uint32_t) * bits.size(), cudaMemcpyHostToDevice, c->st));
+        CU(c, cudaStreamSynchronize(c->st));   // `bits` is local
     }
     CU(c, cudaStreamSynchronize(c->st));
     DevGeo& d = c->dg;
     d.nx = g.nx; d.ny = g.ny; d.nt = g.nt; d.nch = g.nch;
     d.lo = g.lo; d.hi = g.hi; d.gs = g.gs;
     d.sponge_w = g.cfg.sponge_width; d.sponge_max = g.cfg.sponge_max;
-    d.box = c->box; d.emit = c->emit; d.rcv = c->rcv; d.rid = c->rid; d.src = c->src;
+    fill_damp(d);
+    d.box = c->box; d.emit = c->emit; d.rcv = c->rcv; d.rid = c->rid; d.rbits = c->rbits; d.rwords = c->rwords; d.src = c->src;
     d.n_src_steps = g.n_src_steps;
     c->strip = strip_supported(d, g.cfg.profile) && !std::getenv("TOMO_NO_STRIP");
     CU(c, cudaMemsetAsync(c->hist, 0, sizeof(float) * (size_t)P * c->S * N, c->st));
@@ -1202,6 +1218,38 @@ tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* 
     CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     *ms_per_launch = (double)ms / steps;
     if (bytes_per_launch) *bytes_per_launch = (which == 0 ? 16.0 : 20.0) * (double)ng * (double)N;
+    return TOMO_OK;
+}
+
+tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const tomo_schedule* sched,
+                               int32_t iter0, int32_t iters, float** d_f, const float** d_f_true, double* eps_log,
+                               double* seconds) {
+    if (!ctxs || n < 1 || !sched || !d_f || iters < 0) return TOMO_ERR_ARG;
+    for (int i = 0; i < n; ++i) {
+        if (!ctxs[i] || !d_f[i]) return TOMO_ERR_ARG;
+        for (int j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return ctxs[i]->fail(TOMO_ERR_ARG, "a context appears twice in the batch");
+    }
+    std::vector<tomo_status> st(n, TOMO_OK);
+    const auto t0 = std::chrono::steady_clock::now();
+    {
+        std::vector<std::thread> pool;
+        pool.reserve(n);
+        for (int i = 0; i < n; ++i)
+            pool.emplace_back([&, i] {
+                const float* ft = d_f_true ? d_f_true[i] : nullptr;
+                for (int it = 0; it < iters && st[i] == TOMO_OK; ++it) {
+                    tomo_iter_stats s{};
+                    st[i] = tomo_iterate_device(ctxs[i], method, sched, iter0 + it, d_f[i], nullptr, ft, &s);
+                    if (eps_log) eps_log[(int64_t)i * iters + it] = s.epsilon;
+                }
+                if (st[i] == TOMO_OK) st[i] = tomo_synchronize(ctxs[i]);
+            });
+        for (auto& t : pool) t.join();
+    }
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (int i = 0; i < n; ++i)
+        if (st[i] != TOMO_OK) return st[i];
     return TOMO_OK;
 }
 

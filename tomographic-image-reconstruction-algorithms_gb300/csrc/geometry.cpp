@@ -86,7 +86,10 @@ tomo_status build_geometry(const tomo_config& c, Geometry& geo, std::string& why
         }
         if (!(C > 0.0) || C > 0.70710678) { why = "courant must be in (0, 1/sqrt(2)]"; return TOMO_ERR_ARG; }
         if (!(c.cells_per_wavelength >= 2.0f)) { why = "cells_per_wavelength must be >= 2"; return TOMO_ERR_ARG; }
-        if (c.sponge_width < 0 || c.sponge_max < 0.f || c.sponge_max >= 1.f) { why = "bad sponge"; return TOMO_ERR_ARG; }
+        if (c.sponge_width < 0 || c.sponge_width > 64 || c.sponge_max < 0.f || c.sponge_max >= 1.f) {
+            why = "bad sponge (width 0..64, 0 <= max < 1)";
+            return TOMO_ERR_ARG;
+        }
         geo.ii.resize(geo.ns); geo.jj.resize(geo.ns);
         for (int p = 0; p < geo.ns; ++p) {
             const double th = 2.0 * M_PI * p / geo.ns;
@@ -249,6 +252,13 @@ void add_record_noise(float* rec, int G, int nt, int nch, float level, uint64_t 
                 if (amp > 0.0) rec[((int64_t)g * nt + k) * nch + c] += (float)(amp * z);
             }
         }
+}
+
+void fill_damp(DevGeo& g) {
+    for (int dd = 0; dd < 64; ++dd) {
+        const double x = dd < g.sponge_w ? (double)(g.sponge_w - dd) / (double)g.sponge_w : 0.0;
+        g.damp[dd] = (float)(1.0 - (double)g.sponge_max * x * x);
+    }
 }
 
 }  // namespace tomo

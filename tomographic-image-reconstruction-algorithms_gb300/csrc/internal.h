@@ -67,10 +67,13 @@ struct DevGeo {
     int gs;                // CFG emitters per group
     int sponge_w;          // CFG
     float sponge_max;      // CFG
+    float damp[64];        // CFG sponge factor 1 - smax ((w - dd) / w)^2 at distance dd < w from the edge
     const int32_t* box;    // REF per-group emission box (4 ints), global group index
     const int32_t* emit;   // CFG emitter cells, global group index
     const int32_t* rcv;    // receiver cell per channel
     const int32_t* rid;    // CFG per-cell channel or -1
+    const uint32_t* rbits; // CFG per row: bit b set when cells [32b, 32b+32) hold a receiver
+    int rwords;            // words of rbits per row
     const float* src;      // per step source factor
     int n_src_steps;
 };
@@ -143,6 +146,9 @@ void launch_avgw_fbar(const float* corr, int G, int64_t N, const float* f, const
                       double scale, double s, float* fbar, void* stream);
 void launch_avgw_apply(const float* corr, int G, int64_t N, float* f, const uint8_t* mask,
                        double scale, double s, const double* w, void* stream);
+// Fills g.damp from g.sponge_w and g.sponge_max (evaluated in FP64, rounded once).
+void fill_damp(DevGeo& g);
+
 void launch_sum_parts(const double* part, int rows, int nb, double* out, void* stream);
 void launch_maxabs(const float* dir, const uint8_t* mask, int64_t N, unsigned int* out, void* stream);
 void launch_apply(float* f, const float* dir, const uint8_t* mask, int64_t N, double s,

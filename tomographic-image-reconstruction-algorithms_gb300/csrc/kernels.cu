@@ -102,12 +102,8 @@ __global__ void __launch_bounds__(BX * BY) k_fwd(DevGeo g, const float* __restri
         const float so = j > 0 ? uc[q - nx] : 0.f;
         const float no = j + 1 < ny ? uc[q + nx] : 0.f;
         const float lap = (e + w + so + no) - 4.f * u0;
-        float d = 1.f;
         const int dd = min(min(i, j), min(nx - 1 - i, ny - 1 - j));
-        if (dd < g.sponge_w) {
-            const float x = (float)(g.sponge_w - dd) / (float)g.sponge_w;
-            d = 1.f - g.sponge_max * x * x;
-        }
+        const float d = dd < g.sponge_w ? g.damp[dd] : 1.f;
         val = d * ((2.f * u0 - up[q]) + c * lap);
         if (s.k < g.n_src_steps) {
             const int32_t* em = g.emit + (int64_t)(s.g0 + gl) * g.gs;
@@ -191,12 +187,8 @@ __global__ void __launch_bounds__(BX * BY) k_adj(DevGeo g, const float* __restri
         const float lz = (e + w + so + no) - 4.f * c0 * z1[q];
         const int r = g.rid[q];
         const float inj = r >= 0 ? rr[r] : 0.f;
-        float d = 1.f;
         const int dd = min(min(i, j), min(nx - 1 - i, ny - 1 - j));
-        if (dd < g.sponge_w) {
-            const float x = (float)(g.sponge_w - dd) / (float)g.sponge_w;
-            d = 1.f - g.sponge_max * x * x;
-        }
+        const float d = dd < g.sponge_w ? g.damp[dd] : 1.f;
         val = d * ((2.f * z1[q] - z2[q]) + lz + inj);
         const float ue = i + 1 < nx ? u[q + 1] : 0.f;
         const float uw = i > 0 ? u[q - 1] : 0.f;

@@ -122,7 +122,8 @@ extern "C" tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float*
     dg.nx = geo.nx; dg.ny = geo.ny; dg.nt = geo.nt; dg.nch = geo.nch;
     dg.lo = geo.lo; dg.hi = geo.hi; dg.gs = geo.gs;
     dg.sponge_w = cfg->sponge_width; dg.sponge_max = cfg->sponge_max;
-    dg.box = box; dg.emit = emit; dg.rcv = rcv; dg.rid = nullptr; dg.src = src;
+    fill_damp(dg);
+    dg.box = box; dg.emit = emit; dg.rcv = rcv; dg.rid = nullptr; dg.rbits = nullptr; dg.rwords = 0; dg.src = src;
     dg.n_src_steps = geo.n_src_steps;
     const int prof = cfg->profile;
     launch_coef(prof, d_f, coef, rcoef, N, cfg->courant, st);

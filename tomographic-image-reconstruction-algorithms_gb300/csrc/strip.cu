@@ -31,11 +31,10 @@ __device__ __forceinline__ float4 ld4(const float* __restrict__ p, int64_t off, 
     return ok ? *reinterpret_cast<const float4*>(p + off) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__device__ __forceinline__ float sponge(int i, int j, int nx, int ny, int w, float smax) {
-    const int dd = min(min(i, j), min(nx - 1 - i, ny - 1 - j));
-    if (dd >= w) return 1.f;
-    const float x = (float)(w - dd) / (float)w;
-    return 1.f - smax * x * x;
+// Sponge factor of cell (i, j): a table lookup by the distance to the nearest edge.
+__device__ __forceinline__ float sponge(const DevGeo& g, int i, int j) {
+    const int dd = min(min(i, j), min(g.nx - 1 - i, g.ny - 1 - j));
+    return dd < g.sponge_w ? g.damp[dd] : 1.f;
 }
 
 // Adjoint arithmetic with explicit rounding: the one-step and two-step kernels
@@ -43,10 +42,16 @@ __device__ __forceinline__ float sponge(int i, int j, int nx, int ny, int w, flo
 // the compiler would otherwise contract into fused multiply-adds.
 __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
 
-// d * ((2 z - z2) + (((ce + cw) + cs) + cn - 4 c z) + inj), products passed in rounded
-__device__ __forceinline__ float adj_cell(float ce, float cw, float cs, float cn, float c, float z, float z2,
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return make_float2(mul(a.x, b.x), mul(a.y, b.y)); }
+__device__ __forceinline__ float4 mul4(float4 a, float4 b) {
+    return make_float4(mul(a.x, b.x), mul(a.y, b.y), mul(a.z, b.z), mul(a.w, b.w));
+}
+
+// d * ((2 z - z2) + ((((ce + cw) + cs) + cn) - 4 cz) + inj), where cz = c z and the
+// neighbour products c z are passed in rounded (4 cz is exact: a power-of-two scale)
+__device__ __forceinline__ float adj_cell(float ce, float cw, float cs, float cn, float cz, float z, float z2,
                                           float inj, float d) {
-    const float lz = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(ce, cw), cs), cn), mul(mul(4.f, c), z));
+    const float lz = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(ce, cw), cs), cn), mul(4.f, cz));
     return mul(d, __fadd_rn(__fadd_rn(__fsub_rn(mul(2.f, z), z2), lz), inj));
 }
 
@@ -78,6 +83,49 @@ __device__ __forceinline__ void we(const float4& v, const float* __restrict__ ro
     east = __shfl_down_sync(FULL, v.x, 1);
     if (lane == 0) west = x0 > 0 ? row[x0 - 1] : 0.f;
     if (lane == 31) east = x0 + STRIP < nx ? row[x0 + STRIP] : 0.f;
+}
+
+// Receiver bitmap (g.rbits: per row, one bit per 32-cell block, g.rwords words per row) words
+// and masks covering a strip's cells [xa, xb); a strip of at most 128 cells spans at most two
+// words.  Strips whose rows have no receiver never read the per-cell receiver map.
+struct RcvMask {
+    int w0, w1;
+    uint32_t m0, m1;
+};
+
+__device__ __forceinline__ RcvMask rcv_mask(const DevGeo& g, int xa, int xb) {
+    xa = max(xa, 0);
+    xb = min(xb, g.nx);
+    RcvMask k{0, 0, 0u, 0u};
+    if (xa >= xb) return k;
+    const int b0 = xa >> 5, b1 = (xb - 1) >> 5;
+    k.w0 = b0 >> 5;
+    k.w1 = b1 >> 5;
+    const uint32_t lo = ~0u << (b0 & 31);
+    const uint32_t hi = (b1 & 31) == 31 ? ~0u : ((1u << ((b1 & 31) + 1)) - 1u);
+    if (k.w0 == k.w1) {
+        k.m0 = lo & hi;
+    } else {
+        k.m0 = lo;
+        k.m1 = hi;
+    }
+    return k;
+}
+
+// Whether row r has a receiver in the strip (the same answer for the whole warp).
+__device__ __forceinline__ bool rcv_row(const DevGeo& g, const RcvMask& k, int r) {
+    if (r < 0 || r >= g.ny) return false;
+    const uint32_t* w = g.rbits + (int64_t)r * g.rwords;
+    return ((w[k.w0] & k.m0) | (k.m1 ? (w[k.w1] & k.m1) : 0u)) != 0u;
+}
+
+// Distance of index i to the nearer end of [0, n), clamped at 0 for indices outside.
+__device__ __forceinline__ int edge_dist(int i, int n) { return max(0, min(i, n - 1 - i)); }
+
+// Sponge factor from a cell's column and row edge distances (equal to sponge(g, i, j)).
+__device__ __forceinline__ float damp_at(const DevGeo& g, int dcol, int drow) {
+    const int dd = min(dcol, drow);
+    return dd < g.sponge_w ? g.damp[dd] : 1.f;
 }
 
 // ---------------------------------------------------------------------------
@@ -124,10 +172,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_fwd_strip(DevGeo g, const float*
         float w, e;
         we(r0, uc + row, lane, x0, nx, w, e);
         const bool near = edge_x || j < g.sponge_w || j >= ny - g.sponge_w;
-        const float dx = near ? sponge(i, j, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
-        const float dy = near ? sponge(i + 1, j, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
-        const float dz = near ? sponge(i + 2, j, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
-        const float dw = near ? sponge(i + 3, j, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+        const float dx = near ? sponge(g, i, j) : 1.f;
+        const float dy = near ? sponge(g, i + 1, j) : 1.f;
+        const float dz = near ? sponge(g, i + 2, j) : 1.f;
+        const float dw = near ? sponge(g, i + 3, j) : 1.f;
         const int64_t q0 = row + i;
         const float ax = src ? emit_at(em, g.gs, q0, a) : 0.f;
         const float ay = src ? emit_at(em, g.gs, q0 + 1, a) : 0.f;
@@ -168,45 +216,50 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) k_adj_strip(DevGeo g, const 
     const float* rr = s.rr + gl * s.rrstride;
     float* corr = s.corr + gl * s.cstride;
     const bool edge_x = x0 < g.sponge_w || x0 + STRIP > nx - g.sponge_w;
-    // rolling rows: z1, coef*z1 and u
-    float4 zm = ld4(z1, (int64_t)(y0 - 1) * nx + i, act && y0 > 0);
-    float4 cm = ld4(coef, (int64_t)(y0 - 1) * nx + i, act && y0 > 0);
-    float4 z0 = ld4(z1, (int64_t)y0 * nx + i, act);
-    float4 c0 = ld4(coef, (int64_t)y0 * nx + i, act);
-    float4 um = ld4(u, (int64_t)(y0 - 1) * nx + i, act && y0 > 0);
-    float4 u0 = ld4(u, (int64_t)y0 * nx + i, act);
+    const RcvMask rk = rcv_mask(g, x0, x0 + STRIP);
+    const int dc[4] = {edge_dist(i, nx), edge_dist(i + 1, nx), edge_dist(i + 2, nx), edge_dist(i + 3, nx)};
+    // rolling rows: the products c*z(k+1) above and at the row, z(k+1) and u at the row, u above
+    // (32-bit offsets: the strip path requires nx*ny < 2^31)
+    const bool up_ok = act && y0 > 0;
+    const int top = (y0 - 1) * nx + i;
+    float4 pm = mul4(ld4(coef, top, up_ok), ld4(z1, top, up_ok));
+    float4 z0 = ld4(z1, y0 * nx + i, act);
+    float4 p0 = mul4(ld4(coef, y0 * nx + i, act), z0);
+    float4 um = ld4(u, top, up_ok);
+    float4 u0 = ld4(u, y0 * nx + i, act);
 #pragma unroll UNR
     for (int r = 0; r < R; ++r) {
         const int j = y0 + r;
         if (j >= ny) break;
-        const int64_t row = (int64_t)j * nx;
+        const int row = j * nx;
         const bool has_next = act && j + 1 < ny;
         const float4 zp = ld4(z1, row + nx + i, has_next);
-        const float4 cp = ld4(coef, row + nx + i, has_next);
+        const float4 pp = mul4(ld4(coef, row + nx + i, has_next), zp);
         const float4 uq = ld4(u, row + nx + i, has_next);
         const float4 zz = ld4(z2, row + i, act);
-        // coefficient-weighted neighbours of z(k+1): c*z at west/east via shuffles
-        const float4 cz0 = make_float4(mul(c0.x, z0.x), mul(c0.y, z0.y), mul(c0.z, z0.z), mul(c0.w, z0.w));
-        float czw = __shfl_up_sync(FULL, cz0.w, 1), cze = __shfl_down_sync(FULL, cz0.x, 1);
-        if (lane == 0) czw = x0 > 0 ? mul(coef[row + x0 - 1], z1[row + x0 - 1]) : 0.f;
-        if (lane == 31) cze = x0 + STRIP < nx ? mul(coef[row + x0 + STRIP], z1[row + x0 + STRIP]) : 0.f;
-        float v[4];
-        const float czs[4] = {mul(cm.x, zm.x), mul(cm.y, zm.y), mul(cm.z, zm.z), mul(cm.w, zm.w)};
-        const float czn[4] = {mul(cp.x, zp.x), mul(cp.y, zp.y), mul(cp.z, zp.z), mul(cp.w, zp.w)};
-        const float cze4[4] = {cz0.y, cz0.z, cz0.w, cze};
-        const float czw4[4] = {czw, cz0.x, cz0.y, cz0.z};
+        // products at the west/east neighbours via shuffles, one scalar pair at each strip end
+        float pw = __shfl_up_sync(FULL, p0.w, 1), pe = __shfl_down_sync(FULL, p0.x, 1);
+        if (lane == 0) pw = x0 > 0 ? mul(coef[row + x0 - 1], z1[row + x0 - 1]) : 0.f;
+        if (lane == 31) pe = x0 + STRIP < nx ? mul(coef[row + x0 + STRIP], z1[row + x0 + STRIP]) : 0.f;
+        const float ps[4] = {pm.x, pm.y, pm.z, pm.w};
+        const float pn[4] = {pp.x, pp.y, pp.z, pp.w};
+        const float pe4[4] = {p0.y, p0.z, p0.w, pe};
+        const float pw4[4] = {pw, p0.x, p0.y, p0.z};
+        const float pc[4] = {p0.x, p0.y, p0.z, p0.w};
         const float zc[4] = {z0.x, z0.y, z0.z, z0.w};
-        const float cc[4] = {c0.x, c0.y, c0.z, c0.w};
         const float z2v[4] = {zz.x, zz.y, zz.z, zz.w};
         const bool near_y = j < g.sponge_w || j >= ny - g.sponge_w;
-        int4 rid = act ? *reinterpret_cast<const int4*>(g.rid + row + i) : make_int4(-1, -1, -1, -1);
+        const int dr = edge_dist(j, ny);
+        int4 rid = make_int4(-1, -1, -1, -1);
+        if (rcv_row(g, rk, j) && act) rid = *reinterpret_cast<const int4*>(g.rid + row + i);
         const int rids[4] = {rid.x, rid.y, rid.z, rid.w};
+        float v[4];
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
             const float inj = rids[t] >= 0 ? rr[rids[t]] : 0.f;
             float d = 1.f;
-            if (edge_x || near_y) d = sponge(i + t, j, nx, ny, g.sponge_w, g.sponge_max);
-            v[t] = adj_cell(cze4[t], czw4[t], czs[t], czn[t], cc[t], zc[t], z2v[t], inj, d);
+            if (edge_x || near_y) d = damp_at(g, dc[t], dr);
+            v[t] = adj_cell(pe4[t], pw4[t], ps[t], pn[t], pc[t], zc[t], z2v[t], inj, d);
         }
         // Laplacian of the forward slice (zero outside the grid)
         float uw, ue;
@@ -228,8 +281,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) k_adj_strip(DevGeo g, const 
             *reinterpret_cast<float4*>(corr + row + i) = cr;
             *reinterpret_cast<float4*>(zk + row + i) = make_float4(v[0], v[1], v[2], v[3]);
         }
-        zm = z0; z0 = zp;
-        cm = c0; c0 = cp;
+        pm = p0; p0 = pp; z0 = zp;
         um = u0; u0 = uq;
     }
 }
@@ -283,8 +335,10 @@ __device__ __forceinline__ float2 ld2(const float* __restrict__ p, int64_t off, 
     return ok ? *reinterpret_cast<const float2*>(p + off) : make_float2(0.f, 0.f);
 }
 
-template <int R>
-__global__ void __launch_bounds__(WARPS * 32, 8) k_adj2_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
+// PF: read the correlation row one iteration ahead (more registers: 7 blocks per SM).
+template <int R, bool PF>
+__global__ void __launch_bounds__(WARPS * 32, PF ? 7 : 8) k_adj2_strip(DevGeo g, const float* __restrict__ coef,
+                                                                      Adj2Step s) {
     const int nx = g.nx, ny = g.ny;
     const int gl = blockIdx.z;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -294,6 +348,7 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_adj2_strip(DevGeo g, const fl
     if (y0 >= ny) return;
     const bool in = i >= 0 && i < nx;
     const bool own = in && lane >= 1 && lane <= 30;
+    const int yend = min(y0 + R, ny);          // rows y0 .. yend-1 are written
     const float* z1 = s.z1 + gl * s.zstride;
     const float* z2 = s.z2 + gl * s.zstride;
     float* za = s.za + gl * s.zstride;
@@ -305,67 +360,82 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_adj2_strip(DevGeo g, const fl
     float* corr = s.corr + gl * s.cstride;
     const bool edge_x = x0 < g.sponge_w || x0 + 64 > nx - g.sponge_w;
     auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
-    // rolling state at the top of iteration r
-    float2 z1m = ld2(z1, (int64_t)(y0 - 2) * nx + i, row_ok(y0 - 2));
-    float2 z10 = ld2(z1, (int64_t)(y0 - 1) * nx + i, row_ok(y0 - 1));
-    float2 cm2 = make_float2(0.f, 0.f);
-    float2 cm = ld2(coef, (int64_t)(y0 - 2) * nx + i, row_ok(y0 - 2));
-    float2 c0 = ld2(coef, (int64_t)(y0 - 1) * nx + i, row_ok(y0 - 1));
-    float2 zam2 = make_float2(0.f, 0.f), zam = make_float2(0.f, 0.f);
+    const RcvMask rk = rcv_mask(g, x0, x0 + 64);
+    const int dca = edge_dist(i, nx), dcb = edge_dist(i + 1, nx);
+    // rolling state at the top of iteration r (first step at row r, second at row r-1), with
+    // 32-bit offsets (the strip path requires nx*ny < 2^31):
+    //   z(kz+1) at rows r-1 (z1m) and r (z10); products c*z(kz+1) at rows r-1, r (pzm, pz0);
+    //   the coefficient at row r (c0); z(kz) at row r-1 (zam) and its products c*z(kz) at
+    //   rows r-2, r-1 (pam2, pam); u(q), u(q-1) at rows r-2, r-1; receiver ids of row r-1;
+    //   the correlation of row r-1 (read one iteration ahead)
+    float2 z1m = ld2(z1, (y0 - 2) * nx + i, row_ok(y0 - 2));
+    float2 z10 = ld2(z1, (y0 - 1) * nx + i, row_ok(y0 - 1));
+    float2 pzm = mul2(ld2(coef, (y0 - 2) * nx + i, row_ok(y0 - 2)), z1m);
+    float2 c0 = ld2(coef, (y0 - 1) * nx + i, row_ok(y0 - 1));
+    float2 pz0 = mul2(c0, z10);
+    float2 zam = make_float2(0.f, 0.f), pam2 = make_float2(0.f, 0.f), pam = make_float2(0.f, 0.f);
     float2 uam2 = make_float2(0.f, 0.f), uam = make_float2(0.f, 0.f);
     float2 ubm2 = make_float2(0.f, 0.f), ubm = make_float2(0.f, 0.f);
+    float2 crm = make_float2(0.f, 0.f);
     int2 ridm = make_int2(-1, -1);
 #pragma unroll 1
     for (int r = y0 - 1; r <= y0 + R; ++r) {
         if (r > ny) break;
-        const int64_t row = (int64_t)r * nx;
+        const int row = r * nx;
         const bool ok = row_ok(r);
-        const float2 z1p = ld2(z1, row + nx + i, row_ok(r + 1));
-        const float2 cp = ld2(coef, row + nx + i, row_ok(r + 1));
+        const bool okn = row_ok(r + 1);
+        const float2 z1p = ld2(z1, row + nx + i, okn);
+        const float2 cp = ld2(coef, row + nx + i, okn);
         const float2 zz = ld2(z2, row + i, ok);
         const float2 ua0 = ld2(ua, row + i, ok);
         const float2 ub0 = ld2(ub, row + i, ok);
-        const int2 rid = ok ? *reinterpret_cast<const int2*>(g.rid + row + i) : make_int2(-1, -1);
+        int2 rid = make_int2(-1, -1);
+        if (rcv_row(g, rk, r) && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
+        // correlation of row r, read now for the second step of the next iteration
+        float2 cr_next = make_float2(0.f, 0.f);
+        if (PF && own && r >= y0 && r < yend) cr_next = *reinterpret_cast<const float2*>(corr + row + i);
+        const float2 pzp = mul2(cp, z1p);
         // ---- first step: z(kz) at row r (all lanes; zero outside the grid)
         float2 za0 = make_float2(0.f, 0.f);
         {
-            const float cz0x = mul(c0.x, z10.x), cz0y = mul(c0.y, z10.y);
-            float czw = __shfl_up_sync(FULL, cz0y, 1), cze = __shfl_down_sync(FULL, cz0x, 1);
-            if (lane == 0) czw = (ok && x0 > 0) ? mul(coef[row + x0 - 1], z1[row + x0 - 1]) : 0.f;
-            if (lane == 31) cze = (ok && x0 + 64 < nx) ? mul(coef[row + x0 + 64], z1[row + x0 + 64]) : 0.f;
+            float pw = __shfl_up_sync(FULL, pz0.y, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
+            if (lane == 0) pw = (ok && x0 > 0) ? mul(coef[row + x0 - 1], z1[row + x0 - 1]) : 0.f;
+            if (lane == 31) pe = (ok && x0 + 64 < nx) ? mul(coef[row + x0 + 64], z1[row + x0 + 64]) : 0.f;
             if (ok) {
                 const bool near = edge_x || r < g.sponge_w || r >= ny - g.sponge_w;
+                const int dr = edge_dist(r, ny);
                 const float ix = rid.x >= 0 ? rra[rid.x] : 0.f;
                 const float iy = rid.y >= 0 ? rra[rid.y] : 0.f;
-                const float dx = near ? sponge(i, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
-                const float dy = near ? sponge(i + 1, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
-                za0.x = adj_cell(cz0y, czw, mul(cm.x, z1m.x), mul(cp.x, z1p.x), c0.x, z10.x, zz.x, ix, dx);
-                za0.y = adj_cell(cze, cz0x, mul(cm.y, z1m.y), mul(cp.y, z1p.y), c0.y, z10.y, zz.y, iy, dy);
+                const float dx = near ? damp_at(g, dca, dr) : 1.f;
+                const float dy = near ? damp_at(g, dcb, dr) : 1.f;
+                za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, ix, dx);
+                za0.y = adj_cell(pe, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, iy, dy);
             }
         }
+        const float2 pa0 = mul2(c0, za0);
         // ---- second step: z(kz-1) at row r-1, correlation of both steps at row r-1
         const int rb = r - 1;
         {
             // every lane joins the shuffles
-            const float czax = mul(cm.x, zam.x), czay = mul(cm.y, zam.y);
-            const float czw = __shfl_up_sync(FULL, czay, 1), cze = __shfl_down_sync(FULL, czax, 1);
+            const float pw = __shfl_up_sync(FULL, pam.y, 1), pe = __shfl_down_sync(FULL, pam.x, 1);
             const float uaw = __shfl_up_sync(FULL, uam.y, 1), uae = __shfl_down_sync(FULL, uam.x, 1);
             const float ubw = __shfl_up_sync(FULL, ubm.y, 1), ube = __shfl_down_sync(FULL, ubm.x, 1);
             if (own && rb >= y0 && rb < ny) {
                 const bool near = edge_x || rb < g.sponge_w || rb >= ny - g.sponge_w;
-                const int64_t rowb = (int64_t)rb * nx;
+                const int rowb = rb * nx;
+                const int dr = edge_dist(rb, ny);
                 const float ix = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
                 const float iy = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
-                const float dx = near ? sponge(i, rb, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
-                const float dy = near ? sponge(i + 1, rb, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+                const float dx = near ? damp_at(g, dca, dr) : 1.f;
+                const float dy = near ? damp_at(g, dcb, dr) : 1.f;
                 float2 zbv;
-                zbv.x = adj_cell(czay, czw, mul(cm2.x, zam2.x), mul(c0.x, za0.x), cm.x, zam.x, z1m.x, ix, dx);
-                zbv.y = adj_cell(cze, czax, mul(cm2.y, zam2.y), mul(c0.y, za0.y), cm.y, zam.y, z1m.y, iy, dy);
+                zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, ix, dx);
+                zbv.y = adj_cell(pe, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, iy, dy);
                 const float lax = lap5(uam.y, uaw, uam2.x, ua0.x, uam.x);
                 const float lay = lap5(uae, uam.x, uam2.y, ua0.y, uam.y);
                 const float lbx = lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x);
                 const float lby = lap5(ube, ubm.x, ubm2.y, ub0.y, ubm.y);
-                float2 cr = *reinterpret_cast<const float2*>(corr + rowb + i);
+                float2 cr = PF ? crm : *reinterpret_cast<const float2*>(corr + rowb + i);
                 cr.x = __fmaf_rn(zam.x, lax, cr.x);
                 cr.y = __fmaf_rn(zam.y, lay, cr.y);
                 cr.x = __fmaf_rn(zbv.x, lbx, cr.x);
@@ -376,19 +446,22 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_adj2_strip(DevGeo g, const fl
             }
         }
         z1m = z10; z10 = z1p;
-        cm2 = cm; cm = c0; c0 = cp;
-        zam2 = zam; zam = za0;
+        pzm = pz0; pz0 = pzp;
+        c0 = cp;
+        zam = za0;
+        pam2 = pam; pam = pa0;
         uam2 = uam; uam = ua0;
         ubm2 = ubm; ubm = ub0;
         ridm = rid;
+        crm = cr_next;
     }
 }
 
-template <int R>
+template <int R, bool PF>
 void adj2_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     dim3 grid((g.nx + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
-    k_adj2_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+    k_adj2_strip<R, PF><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -470,8 +543,8 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_fwd2_strip(DevGeo g, const fl
         float2 v10 = make_float2(0.f, 0.f);
         if (ok) {
             const bool near = edge_x || r < g.sponge_w || r >= ny - g.sponge_w;
-            const float dx = near ? sponge(i, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
-            const float dy = near ? sponge(i + 1, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+            const float dx = near ? sponge(g, i, r) : 1.f;
+            const float dy = near ? sponge(g, i + 1, r) : 1.f;
             const float ax = src1 ? emit_at(em, g.gs, row + i, a1) : 0.f;
             const float ay = src1 ? emit_at(em, g.gs, row + i + 1, a1) : 0.f;
             v10.x = fwd_cell(u00.y, w, u0m.x, u0p.x, u00.x, p.x, c0.x, dx, ax);
@@ -483,8 +556,8 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_fwd2_strip(DevGeo g, const fl
         if (own && rb >= y0 && rb < ny) {
             const int64_t rowb = (int64_t)rb * nx;
             const bool near = edge_x || rb < g.sponge_w || rb >= ny - g.sponge_w;
-            const float dx = near ? sponge(i, rb, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
-            const float dy = near ? sponge(i + 1, rb, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+            const float dx = near ? sponge(g, i, rb) : 1.f;
+            const float dy = near ? sponge(g, i + 1, rb) : 1.f;
             const float ax = src2 ? emit_at(em, g.gs, rowb + i, a2) : 0.f;
             const float ay = src2 ? emit_at(em, g.gs, rowb + i + 1, a2) : 0.f;
             float2 v2;
@@ -546,7 +619,7 @@ __global__ void __launch_bounds__(WARPS * 32, 6) k_fwd2q_strip(DevGeo g, const f
         const bool near = edge_x || r < g.sponge_w || r >= ny - g.sponge_w;
         const int64_t q = (int64_t)r * nx + i;
         for (int t = 0; t < 4; ++t) {
-            d[t] = near ? sponge(i + t, r, nx, ny, g.sponge_w, g.sponge_max) : 1.f;
+            d[t] = near ? sponge(g, i + t, r) : 1.f;
             a[t] = srcf ? emit_at(em, g.gs, q + t, amp) : 0.f;
         }
     };
@@ -629,7 +702,11 @@ void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, 
     k_resid_parts<<<dim3(nt, ng), 256, 0, (cudaStream_t)stream>>>(rr, nt, nch, part);
 }
 
-bool strip_supported(const DevGeo& g, int profile) { return profile == TOMO_PROFILE_CFG && g.nx % 4 == 0; }
+// The strip kernels index a slice with 32-bit offsets.
+bool strip_supported(const DevGeo& g, int profile) {
+    return profile == TOMO_PROFILE_CFG && g.nx % 4 == 0 && (int64_t)g.nx * (g.ny + 2) < ((int64_t)1 << 31) &&
+           g.rbits != nullptr;
+}
 
 void launch_fwd2_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& a, const FwdStep& b,
                        bool gather_prev, bool gather_cur, void* stream) {
@@ -661,11 +738,15 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     s.rra = a.rr; s.rrb = b.rr; s.rrstride = a.rrstride;
     s.corr = a.corr; s.cstride = a.cstride; s.ng = a.ng;
     cudaStream_t st = (cudaStream_t)stream;
-    switch (rows) {
-    case 4: adj2_strip<4>(g, coef, s, st); break;
-    case 16: adj2_strip<16>(g, coef, s, st); break;
-    case 32: adj2_strip<32>(g, coef, s, st); break;
-    default: adj2_strip<8>(g, coef, s, st); break;
+    switch (rows) {   // rows + 100: the variant that reads the correlation one row ahead
+    case 4: adj2_strip<4, false>(g, coef, s, st); break;
+    case 16: adj2_strip<16, false>(g, coef, s, st); break;
+    case 32: adj2_strip<32, false>(g, coef, s, st); break;
+    case 104: adj2_strip<4, true>(g, coef, s, st); break;
+    case 108: adj2_strip<8, true>(g, coef, s, st); break;
+    case 116: adj2_strip<16, true>(g, coef, s, st); break;
+    case 132: adj2_strip<32, true>(g, coef, s, st); break;
+    default: adj2_strip<8, false>(g, coef, s, st); break;
     }
 }
 

@@ -17,7 +17,9 @@ Pipeline, all compute in libtomo.so's kernels (torch only holds device buffers):
      tomo_run_learned) runs until it reaches the plain method's final image
      error.
 
-Usage:  python learn.py [--phantoms 1000] [--iters 20] [--epochs 8] [--out weights.bin]
+Usage:  python learn.py [--phantoms 400] [--iters 36] [--lookahead 6] [--epochs 12]
+                        [--onpolicy-phantoms 200] [--out weights.bin]
+        python learn.py --eval-only --out weights.bin --eval-seeds 2001,2002
 """
 from __future__ import annotations
 
@@ -96,6 +98,60 @@ def generate(n_phantoms, iters, lookahead=6, seed0=4000, device=0, target="looka
                 log(f"  data: phantom {ph}/{n_phantoms}, {time.time() - t0:.1f} s")
     torch.cuda.synchronize(dev)
     return feats, tgts, m, time.time() - t0
+
+
+def generate_onpolicy(net, n_phantoms, iters, lookahead=6, seed0=9000, device=0, log=print):
+    """States the learned iteration itself visits (the residual-checked rule of tomo_run_learned
+    with a window of one), each paired with the field change of `lookahead` plain weighted-SIRT
+    steps taken from that state; a network trained on plain trajectories alone drifts off them.
+    Returns (features [M,3,H,W], targets [M,H,W]), M = n_phantoms * iters."""
+    import torch
+
+    dev = torch.device("cuda", device)
+    cfg = train_config(device)
+    m = torch.from_numpy(mask_of(cfg)).to(dev)
+    H, W = cfg.ny, cfg.nx
+    M = n_phantoms * iters
+    feats = torch.empty((M, 3, H, W), dtype=torch.float32, device=dev)
+    tgts = torch.empty((M, H, W), dtype=torch.float32, device=dev)
+    cur = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+    nxt = torch.empty_like(cur)
+    tmp = torch.empty_like(cur)
+    out = torch.empty((1, H, W), dtype=torch.float32, device=dev)
+    t0 = time.time()
+    j, acc = 0, 0
+    with tomo.Context(cfg) as ctx:
+        for ph in range(n_phantoms):
+            fo = phantom(cfg, seed0 + ph, *TRAIN_RADII)
+            ctx.set_records(ctx.generate_data(fo, noise_level=0.01, seed=seed0 + ph))
+            f = torch.zeros((H, W), dtype=torch.float32, device=dev)
+            torch.cuda.synchronize(dev)
+            r0 = ctx.features_device(f.data_ptr(), cur.data_ptr())
+            for t in range(iters):
+                feats[j] = cur
+                g = f + STEP * m * cur[1]
+                for _ in range(lookahead - 1):
+                    torch.cuda.synchronize(dev)
+                    ctx.features_device(g.data_ptr(), tmp.data_ptr())
+                    g = g + STEP * m * tmp[1]
+                tgts[j] = g - f
+                j += 1
+                torch.cuda.synchronize(dev)
+                net.forward_device(cur.data_ptr(), 1, H, W, out.data_ptr())
+                fp = f + m * out[0]
+                torch.cuda.synchronize(dev)
+                r1 = ctx.features_device(fp.data_ptr(), nxt.data_ptr())
+                if r1 < r0:
+                    f, r0, acc = fp, r1, acc + 1
+                    cur, nxt = nxt, cur
+                else:
+                    f = f + STEP * m * cur[1]
+                    torch.cuda.synchronize(dev)
+                    r0 = ctx.features_device(f.data_ptr(), cur.data_ptr())
+            if ph % 50 == 0:
+                log(f"  on-policy data: phantom {ph}/{n_phantoms}, {acc}/{j} accepted, {time.time() - t0:.1f} s")
+    torch.cuda.synchronize(dev)
+    return feats, tgts, time.time() - t0
 
 
 def masked_mse(out, tgts, mask):
@@ -210,8 +266,13 @@ def main():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--onpolicy-phantoms", type=int, default=0)
+    ap.add_argument("--onpolicy-iters", type=int, default=20)
     ap.add_argument("--eval-only", action="store_true")
+    ap.add_argument("--eval-seeds", default="2001", help="comma-separated phantom seeds of the evaluation")
     args = ap.parse_args()
+    import torch
+
     net = tomo.Net(0, seed=7)
     report = {}
     if not args.eval_only:
@@ -230,12 +291,30 @@ def main():
         report["train_seconds"] = t_train
         report["val_loss"] = evaluate(net, fv, tv, m)
         print(f"  held-out loss {report['val_loss']:.3e}")
-        os.makedirs(os.path.dirname(args.out), exist_ok=True)
+        if args.onpolicy_phantoms > 0:
+            # a second round on the states the trained network's own iteration visits
+            os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+            net.save(args.out + ".round1")
+            fo_, to_, t_on = generate_onpolicy(net, args.onpolicy_phantoms, args.onpolicy_iters, args.lookahead)
+            report["onpolicy_pairs"] = int(fo_.shape[0])
+            report["onpolicy_seconds"] = t_on
+            feats, tgts = torch.cat([feats, fo_]), torch.cat([tgts, to_])
+            del fo_, to_
+            net = tomo.Net(0, seed=7)
+            losses, t_train = train(net, feats, tgts, m, args.epochs, args.batch, args.lr, seed=1)
+            report["losses_round2"] = losses
+            report["train_seconds"] += t_train
+            report["val_loss_round2"] = evaluate(net, fv, tv, m)
+            print(f"  held-out loss after the on-policy round {report['val_loss_round2']:.3e}")
+        os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
         net.save(args.out)
         del feats, tgts, fv, tv
     else:
         net.load(args.out)
-    report["time_to_image"] = time_to_image(net, windows=(1,))
+    report["time_to_image"] = {}
+    for seed in [int(x) for x in args.eval_seeds.split(",")]:
+        print(f"  evaluation phantom seed {seed}")
+        report["time_to_image"][str(seed)] = time_to_image(net, seed=seed, windows=(1,))
     print(json.dumps(report))
 
 

@@ -175,6 +175,8 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_iterate_learned": (i32, [vp, vp, C.POINTER(Schedule), i32, vp, vp, C.POINTER(IterStats), IP]),
         "tomo_run_learned": (i32, [vp, vp, C.POINTER(Schedule), vp, vp, C.c_double, i32, i32, DP, IP, IP,
                                    C.POINTER(C.c_double)]),
+        "tomo_iterate_batch": (i32, [C.POINTER(vp), i32, i32, C.POINTER(Schedule), i32, i32, C.POINTER(vp),
+                                     C.POINTER(vp), DP, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -351,6 +353,22 @@ class Context:
     @property
     def stream(self) -> int:
         return lib().tomo_stream(self.h) or 0
+
+
+def iterate_batch(ctxs, method, sched: Schedule, iter0: int, iters: int, d_fs, d_ftrues=None):
+    """Advance several contexts together (one host thread each, kernels overlapping on the GPU):
+    (epsilon [n, iters] or NaN without d_ftrues, wall seconds)."""
+    n = len(ctxs)
+    hs = (C.c_void_p * n)(*[c.h for c in ctxs])
+    fs = (C.c_void_p * n)(*d_fs)
+    ts = (C.c_void_p * n)(*d_ftrues) if d_ftrues is not None else None
+    eps = np.full((n, max(iters, 1)), np.nan)
+    secs = C.c_double()
+    st = lib().tomo_iterate_batch(hs, n, method, C.byref(sched), iter0, iters, fs, ts, _dp(eps), C.byref(secs))
+    if st != OK:
+        msgs = [lib().tomo_last_error(c.h) for c in ctxs]
+        raise TomoError(st, "; ".join(m.decode() for m in msgs if m))
+    return eps[:, :iters], secs.value
 
 
 class Net:
