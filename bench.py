@@ -14,7 +14,8 @@ metric: stencil GB/s, algorithmic bytes per iteration = G*nx*ny*(nt-2)*(16+20)
 On c2 the line also carries time_to_image: wall time of 30 plain weighted SIRT
 iterations from f = 0 against the learned update (the shipped network in
 weights/learned_update.bin, residual-checked) run until it reaches the same
-image error, with the speed-up and the gradient sweeps each used.
+image error, with the speed-up, the gradient sweeps each used and the learned
+run's steps (L learned, x rejected proposal + plain step, p plain step).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl tomo|reference]
                     [--workload c2|c1|c3|ref192|c5] [--no-cpu] [--no-learned]
@@ -317,14 +318,16 @@ def time_to_image(ctx, w, sched, d_f, d_ft, torch, dev, plain_iters=30):
     ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), -1.0, 1)    # warm-up: illumination, graphs
     d_f.zero_()
     torch.cuda.synchronize(dev)
-    leps, acc, t_learned = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), eps[-1], 3 * plain_iters)
+    leps, kind, sweeps, t_learned = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), eps[-1],
+                                                    3 * plain_iters)
     net.close()
     reached = bool(leps[-1] <= eps[-1])
-    n_acc = int(acc.sum())
     return {"plain_seconds": t_plain, "plain_iters": plain_iters, "target_epsilon": eps[-1],
-            "learned_seconds": t_learned, "learned_iters": len(leps), "learned_accepted": n_acc,
+            "learned_seconds": t_learned, "learned_iters": len(leps),
+            "learned_steps": "".join({1: "L", 0: "x", -1: "p"}[int(k)] for k in kind),
             "learned_epsilon": float(leps[-1]), "reached": reached,
-            "gradient_sweeps": {"plain": plain_iters, "learned": 1 + len(leps) + (len(leps) - n_acc)},
+            "acceptance": {"min_decrease": tomo.LEARNED_MIN_DECREASE, "patience": tomo.LEARNED_PATIENCE},
+            "gradient_sweeps": {"plain": plain_iters, "learned": sweeps},
             "speedup": t_plain / t_learned if reached else None}
 
 

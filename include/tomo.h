@@ -257,18 +257,21 @@ tomo_status tomo_iterate_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedu
  * iteration proposes f + mask * net(features); the gradient sweep of the
  * proposal is its residual check and, when it passes, also the next
  * iteration's gradient, so an accepted step costs one gradient sweep.  The
- * check passes when the squared record residual of the proposal is below the
- * largest residual of the last `window` fields (1: below the current field's;
- * 2 admits the period-two alternation of plain SIRT's own residual; 1..64).  A
+ * check passes when the squared record residual of the proposal is at most
+ * (1 - min_decrease) times the current field's (0 <= min_decrease < 1).  A
  * rejected proposal falls back to the plain weighted-SIRT step from the saved
- * field (TOMO_SIRT_NORM with `fallback`).  Per iteration eps_log gets the image
- * error (NaN without d_f_true) and accepted_log 1 or 0 (both optional, at least
- * max_iters entries); *seconds is the host wall time of the loop after the
- * one-off illumination sweep.  The counterpart of tomo_run for the learned
- * update; the reference has none. */
+ * field (TOMO_SIRT_NORM with `fallback`); after `patience` consecutive
+ * rejections (0: never) the run stops proposing and continues with plain
+ * steps only.  Per iteration eps_log gets the image error (NaN without
+ * d_f_true) and step_log 1 (learned step), 0 (rejected proposal, plain step)
+ * or -1 (plain step, no proposal); both optional, at least max_iters entries.
+ * *sweeps counts the gradient sweeps (forward + adjoint of all groups) the run
+ * made, *seconds its host wall time after the one-off illumination sweep.  The
+ * counterpart of tomo_run for the learned update; the reference has none. */
 tomo_status tomo_run_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedule* fallback, float* d_f,
-                             const float* d_f_true, double target_epsilon, int32_t max_iters, int32_t window,
-                             double* eps_log, int32_t* accepted_log, int32_t* iters_done, double* seconds);
+                             const float* d_f_true, double target_epsilon, int32_t max_iters, double min_decrease,
+                             int32_t patience, double* eps_log, int32_t* step_log, int32_t* iters_done,
+                             int32_t* sweeps, double* seconds);
 
 /* Several independent reconstructions advanced together (the batched
  * many-phantom workload: phantoms of different grid sizes, each its own

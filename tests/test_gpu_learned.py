@@ -146,8 +146,9 @@ def test_run_learned_rejecting_network_is_plain_sirt(torch_dev):
         net.set_params(np.zeros(net.n_params, np.float32))
         d_f = torch.zeros(fo.shape, dtype=torch.float32, device=dev)
         d_ft = torch.from_numpy(fo).to(dev)
-        eps, acc, secs = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), -1.0, 4)
-        assert len(eps) == 4 and not acc.any() and secs > 0
+        eps, kind, sweeps, secs = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), -1.0, 4)
+        # two rejected proposals (each a wasted sweep plus the plain step), then plain steps only
+        assert list(kind) == [0, 0, -1, -1] and sweeps == 1 + 2 * 2 + 2 and secs > 0
         assert np.array_equal(d_f.cpu().numpy(), f_plain)
         assert list(eps) == eps_plain
 
@@ -165,12 +166,13 @@ def test_run_learned_stops_at_target(torch_dev):
         net.set_params(p)
         d_f = torch.zeros(fo.shape, dtype=torch.float32, device=dev)
         d_ft = torch.from_numpy(fo).to(dev)
-        eps, acc, _ = ctx.run_learned(net, tomo.schedule(omega=0.02, normalize=1), d_f.data_ptr(),
-                                      d_ft.data_ptr(), 1e-2, 10)
-        assert len(eps) == 1 and acc[0] and eps[0] < 1e-2
-        with pytest.raises(tomo.TomoError):
-            ctx.run_learned(net, tomo.schedule(omega=0.02, normalize=1), d_f.data_ptr(), d_ft.data_ptr(),
-                            1e-2, 10, window=0)
+        eps, kind, sweeps, _ = ctx.run_learned(net, tomo.schedule(omega=0.02, normalize=1), d_f.data_ptr(),
+                                               d_ft.data_ptr(), 1e-2, 10)
+        assert len(eps) == 1 and kind[0] == 1 and sweeps == 2 and eps[0] < 1e-2
+        for bad in (dict(min_decrease=1.0), dict(min_decrease=-0.1), dict(patience=-1)):
+            with pytest.raises(tomo.TomoError):
+                ctx.run_learned(net, tomo.schedule(omega=0.02, normalize=1), d_f.data_ptr(), d_ft.data_ptr(),
+                                1e-2, 10, **bad)
 
 
 def test_shipped_network_gain(torch_dev):
@@ -198,7 +200,6 @@ def test_shipped_network_gain(torch_dev):
         net.load(weights)
         d_f.zero_()
         torch.cuda.synchronize(dev)
-        eps, acc, _ = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), target, 30)
-        sweeps = 1 + len(eps) + int((~acc).sum())
+        eps, kind, sweeps, _ = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), target, 30)
         assert eps[-1] <= target, (list(eps), target)
-        assert sweeps <= 15, (sweeps, list(eps), list(acc))
+        assert sweeps <= 15, (sweeps, list(eps), list(kind))

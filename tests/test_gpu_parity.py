@@ -245,8 +245,8 @@ def test_two_step_kernels_match_one_step(nt, monkeypatch):
     meas = O.forward(cfg0, fo.astype(np.float64))
     f0 = blob_phantom(64, 72, seed=9, amp=0.01)
     outs = []
-    # fwd 104: four cells per lane; adj 104: correlation read one row ahead
-    for pair, fwd_rows, adj_rows in (("0", "4", "4"), ("1", "4", "4"), ("1", "104", "104")):
+    # fwd 104: four cells per lane; adj 104 / 208: correlation / all inputs read one row ahead
+    for pair, fwd_rows, adj_rows in (("0", "4", "4"), ("1", "4", "4"), ("1", "104", "104"), ("1", "4", "208")):
         monkeypatch.setenv("TOMO_STRIP_ROWS", "4")
         monkeypatch.setenv("TOMO_FWD_PAIR", pair)
         monkeypatch.setenv("TOMO_FWD_PAIR_ROWS", fwd_rows)

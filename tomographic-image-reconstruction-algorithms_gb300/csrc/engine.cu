@@ -281,7 +281,7 @@ tomo_status autotune(tomo_ctx* c) {
             }
             if (ms < best_f) { best_f = ms; c->rows_fwd2 = code; c->fwd_pair = true; }
         }
-        for (int code : {rows, 100 + rows}) {   // two steps per launch: reps/2 launches cover the same steps
+        for (int code : {rows, 100 + rows, 200 + rows}) {   // two steps per launch: reps/2 launches cover the same steps
             if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {
@@ -1125,9 +1125,11 @@ tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule
 }
 
 tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fallback, float* d_f,
-                             const float* d_f_true, double target_epsilon, int32_t max_iters, int32_t window,
-                             double* eps_log, int32_t* accepted_log, int32_t* iters_done, double* seconds) {
-    if (!c || !net || !fallback || !d_f || max_iters < 0 || window < 1 || window > 64)
+                             const float* d_f_true, double target_epsilon, int32_t max_iters, double min_decrease,
+                             int32_t patience, double* eps_log, int32_t* step_log, int32_t* iters_done,
+                             int32_t* sweeps, double* seconds) {
+    if (!c || !net || !fallback || !d_f || max_iters < 0 || !(min_decrease >= 0.0 && min_decrease < 1.0) ||
+        patience < 0)
         return c ? c->fail(TOMO_ERR_ARG, "bad tomo_run_learned arguments") : TOMO_ERR_ARG;
     if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
     CU(c, cudaSetDevice(c->dev));
@@ -1141,35 +1143,43 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
     const auto t0 = std::chrono::steady_clock::now();
     double r0 = 0.0, r1 = 0.0;
     TRY(features_core(c, &r0));            // gradient, direction and features at the start field
-    std::vector<double> hist(1, r0);       // residuals of the last `window` fields
-    int done = 0;
+    int done = 0, nsweep = 1, rejected = 0;
+    bool learning = true;
     for (int it = 0; it < max_iters; ++it) {
         const double s = sched_scale(fallback, it);
         if (!std::isfinite(s)) return c->fail(TOMO_ERR_ARG, "bad schedule");
-        tomo_status ns = net_infer(net, c->feat, g.ny, g.nx, c->dnet, c->st);
-        if (ns != TOMO_OK) return c->fail(ns, "network: %s", tomo_net_last_error(net));
-        CU(c, cudaMemcpyAsync(c->fsave, c->f, fb, cudaMemcpyDeviceToDevice, c->st));
-        CU(c, cudaMemcpyAsync(c->dsave, c->dir, fb, cudaMemcpyDeviceToDevice, c->st));
-        CU(c, cudaMemcpyAsync(c->maxsave, c->maxabs, sizeof(unsigned int), cudaMemcpyDeviceToDevice, c->st));
-        launch_apply(c->f, c->dnet, c->mask, N, 1.0, nullptr, c->st);
-        c->launches += 7;
-        // the check is the gradient sweep of the proposal: accepted, it is the next step's gradient
-        TRY(features_core(c, &r1));
-        const bool ok = r1 < *std::max_element(hist.begin(), hist.end());
-        if (ok) {
+        int kind = -1;                     // 1 accepted, 0 rejected (plain step), -1 plain step only
+        if (learning) {
+            tomo_status ns = net_infer(net, c->feat, g.ny, g.nx, c->dnet, c->st);
+            if (ns != TOMO_OK) return c->fail(ns, "network: %s", tomo_net_last_error(net));
+            CU(c, cudaMemcpyAsync(c->fsave, c->f, fb, cudaMemcpyDeviceToDevice, c->st));
+            CU(c, cudaMemcpyAsync(c->dsave, c->dir, fb, cudaMemcpyDeviceToDevice, c->st));
+            CU(c, cudaMemcpyAsync(c->maxsave, c->maxabs, sizeof(unsigned int), cudaMemcpyDeviceToDevice, c->st));
+            launch_apply(c->f, c->dnet, c->mask, N, 1.0, nullptr, c->st);
+            c->launches += 7;
+            // the check is the gradient sweep of the proposal: accepted, it is the next step's gradient
+            TRY(features_core(c, &r1));
+            ++nsweep;
+            kind = r1 <= (1.0 - min_decrease) * r0 ? 1 : 0;
+        }
+        if (kind == 1) {
             r0 = r1;
+            rejected = 0;
         } else {
-            CU(c, cudaMemcpyAsync(c->f, c->fsave, fb, cudaMemcpyDeviceToDevice, c->st));
-            launch_apply(c->f, c->dsave, c->mask, N, s, fallback->normalize ? c->maxsave : nullptr, c->st);
+            // plain weighted-SIRT step: from the saved field after a rejected proposal, else from f
+            if (kind == 0) CU(c, cudaMemcpyAsync(c->f, c->fsave, fb, cudaMemcpyDeviceToDevice, c->st));
+            const float* dir = kind == 0 ? c->dsave : c->dir;
+            const unsigned int* mx = kind == 0 ? c->maxsave : c->maxabs;
+            launch_apply(c->f, dir, c->mask, N, s, fallback->normalize ? mx : nullptr, c->st);
             ++c->launches;
             TRY(features_core(c, &r0));
+            ++nsweep;
+            if (kind == 0 && patience > 0 && ++rejected >= patience) learning = false;   // plain from here on
         }
-        hist.push_back(r0);
-        if ((int)hist.size() > window) hist.erase(hist.begin());
         double eps = std::numeric_limits<double>::quiet_NaN();
         if (d_f_true) TRY(epsilon(c, &eps));
         if (eps_log) eps_log[it] = eps;
-        if (accepted_log) accepted_log[it] = ok ? 1 : 0;
+        if (step_log) step_log[it] = kind;
         done = it + 1;
         if (d_f_true && eps <= target_epsilon) break;
     }
@@ -1177,6 +1187,7 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
     CU(c, cudaStreamSynchronize(c->st));
     CU(c, cudaGetLastError());
     if (iters_done) *iters_done = done;
+    if (sweeps) *sweeps = nsweep;
     if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return TOMO_OK;
 }

@@ -335,10 +335,13 @@ __device__ __forceinline__ float2 ld2(const float* __restrict__ p, int64_t off, 
     return ok ? *reinterpret_cast<const float2*>(p + off) : make_float2(0.f, 0.f);
 }
 
-// PF: read the correlation row one iteration ahead (more registers: 7 blocks per SM).
-template <int R, bool PF>
-__global__ void __launch_bounds__(WARPS * 32, PF ? 7 : 8) k_adj2_strip(DevGeo g, const float* __restrict__ coef,
-                                                                      Adj2Step s) {
+// AHEAD: 0 reads each row's inputs in the iteration that uses them; 1 also reads the
+// correlation row one iteration ahead; 2 reads every input one iteration ahead (more loads in
+// flight per warp, more registers: 8 / 7 / 5 blocks per SM).
+template <int R, int AHEAD>
+__global__ void __launch_bounds__(WARPS * 32, AHEAD == 2 ? 5 : 8 - AHEAD) k_adj2_strip(DevGeo g, const float* __restrict__ coef,
+                                                                     Adj2Step s) {
+    constexpr bool PF = AHEAD >= 1;
     const int nx = g.nx, ny = g.ny;
     const int gl = blockIdx.z;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -378,19 +381,45 @@ __global__ void __launch_bounds__(WARPS * 32, PF ? 7 : 8) k_adj2_strip(DevGeo g,
     float2 ubm2 = make_float2(0.f, 0.f), ubm = make_float2(0.f, 0.f);
     float2 crm = make_float2(0.f, 0.f);
     int2 ridm = make_int2(-1, -1);
+    // AHEAD == 2: the inputs of the coming iteration (rows r+1 of z(kz+1) and the coefficient,
+    // rows r of z(kz+2), u(q), u(q-1) and the receiver ids)
+    float2 q_z1 = make_float2(0.f, 0.f), q_c = q_z1, q_zz = q_z1, q_ua = q_z1, q_ub = q_z1;
+    int2 q_rid = make_int2(-1, -1);
+    if (AHEAD == 2) {
+        const int r = y0 - 1, row = r * nx;
+        q_z1 = ld2(z1, row + nx + i, row_ok(r + 1));
+        q_c = ld2(coef, row + nx + i, row_ok(r + 1));
+        q_zz = ld2(z2, row + i, row_ok(r));
+        q_ua = ld2(ua, row + i, row_ok(r));
+        q_ub = ld2(ub, row + i, row_ok(r));
+        if (rcv_row(g, rk, r) && row_ok(r)) q_rid = *reinterpret_cast<const int2*>(g.rid + row + i);
+    }
 #pragma unroll 1
     for (int r = y0 - 1; r <= y0 + R; ++r) {
         if (r > ny) break;
         const int row = r * nx;
         const bool ok = row_ok(r);
-        const bool okn = row_ok(r + 1);
-        const float2 z1p = ld2(z1, row + nx + i, okn);
-        const float2 cp = ld2(coef, row + nx + i, okn);
-        const float2 zz = ld2(z2, row + i, ok);
-        const float2 ua0 = ld2(ua, row + i, ok);
-        const float2 ub0 = ld2(ub, row + i, ok);
+        float2 z1p, cp, zz, ua0, ub0;
         int2 rid = make_int2(-1, -1);
-        if (rcv_row(g, rk, r) && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
+        if (AHEAD == 2) {
+            z1p = q_z1; cp = q_c; zz = q_zz; ua0 = q_ua; ub0 = q_ub; rid = q_rid;
+            const int rn = r + 1, rown = row + nx;
+            q_z1 = ld2(z1, rown + nx + i, row_ok(rn + 1));
+            q_c = ld2(coef, rown + nx + i, row_ok(rn + 1));
+            q_zz = ld2(z2, rown + i, row_ok(rn));
+            q_ua = ld2(ua, rown + i, row_ok(rn));
+            q_ub = ld2(ub, rown + i, row_ok(rn));
+            q_rid = make_int2(-1, -1);
+            if (rcv_row(g, rk, rn) && row_ok(rn)) q_rid = *reinterpret_cast<const int2*>(g.rid + rown + i);
+        } else {
+            const bool okn = row_ok(r + 1);
+            z1p = ld2(z1, row + nx + i, okn);
+            cp = ld2(coef, row + nx + i, okn);
+            zz = ld2(z2, row + i, ok);
+            ua0 = ld2(ua, row + i, ok);
+            ub0 = ld2(ub, row + i, ok);
+            if (rcv_row(g, rk, r) && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
+        }
         // correlation of row r, read now for the second step of the next iteration
         float2 cr_next = make_float2(0.f, 0.f);
         if (PF && own && r >= y0 && r < yend) cr_next = *reinterpret_cast<const float2*>(corr + row + i);
@@ -457,11 +486,11 @@ __global__ void __launch_bounds__(WARPS * 32, PF ? 7 : 8) k_adj2_strip(DevGeo g,
     }
 }
 
-template <int R, bool PF>
+template <int R, int AHEAD>
 void adj2_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     dim3 grid((g.nx + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
-    k_adj2_strip<R, PF><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+    k_adj2_strip<R, AHEAD><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -738,15 +767,19 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     s.rra = a.rr; s.rrb = b.rr; s.rrstride = a.rrstride;
     s.corr = a.corr; s.cstride = a.cstride; s.ng = a.ng;
     cudaStream_t st = (cudaStream_t)stream;
-    switch (rows) {   // rows + 100: the variant that reads the correlation one row ahead
-    case 4: adj2_strip<4, false>(g, coef, s, st); break;
-    case 16: adj2_strip<16, false>(g, coef, s, st); break;
-    case 32: adj2_strip<32, false>(g, coef, s, st); break;
-    case 104: adj2_strip<4, true>(g, coef, s, st); break;
-    case 108: adj2_strip<8, true>(g, coef, s, st); break;
-    case 116: adj2_strip<16, true>(g, coef, s, st); break;
-    case 132: adj2_strip<32, true>(g, coef, s, st); break;
-    default: adj2_strip<8, false>(g, coef, s, st); break;
+    switch (rows) {   // rows + 100 * AHEAD (inputs read one iteration ahead, see k_adj2_strip)
+    case 4: adj2_strip<4, 0>(g, coef, s, st); break;
+    case 16: adj2_strip<16, 0>(g, coef, s, st); break;
+    case 32: adj2_strip<32, 0>(g, coef, s, st); break;
+    case 104: adj2_strip<4, 1>(g, coef, s, st); break;
+    case 108: adj2_strip<8, 1>(g, coef, s, st); break;
+    case 116: adj2_strip<16, 1>(g, coef, s, st); break;
+    case 132: adj2_strip<32, 1>(g, coef, s, st); break;
+    case 204: adj2_strip<4, 2>(g, coef, s, st); break;
+    case 208: adj2_strip<8, 2>(g, coef, s, st); break;
+    case 216: adj2_strip<16, 2>(g, coef, s, st); break;
+    case 232: adj2_strip<32, 2>(g, coef, s, st); break;
+    default: adj2_strip<8, 0>(g, coef, s, st); break;
     }
 }
 

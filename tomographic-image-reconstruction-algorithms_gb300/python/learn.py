@@ -101,8 +101,8 @@ def generate(n_phantoms, iters, lookahead=6, seed0=4000, device=0, target="looka
 
 
 def generate_onpolicy(net, n_phantoms, iters, lookahead=6, seed0=9000, device=0, log=print):
-    """States the learned iteration itself visits (the residual-checked rule of tomo_run_learned
-    with a window of one), each paired with the field change of `lookahead` plain weighted-SIRT
+    """States the learned iteration itself visits (the residual check of tomo_run_learned, proposing
+    at every state), each paired with the field change of `lookahead` plain weighted-SIRT
     steps taken from that state; a network trained on plain trajectories alone drifts off them.
     Returns (features [M,3,H,W], targets [M,H,W]), M = n_phantoms * iters."""
     import torch
@@ -141,7 +141,7 @@ def generate_onpolicy(net, n_phantoms, iters, lookahead=6, seed0=9000, device=0,
                 fp = f + m * out[0]
                 torch.cuda.synchronize(dev)
                 r1 = ctx.features_device(fp.data_ptr(), nxt.data_ptr())
-                if r1 < r0:
+                if r1 <= (1.0 - tomo.LEARNED_MIN_DECREASE) * r0:
                     f, r0, acc = fp, r1, acc + 1
                     cur, nxt = nxt, cur
                 else:
@@ -207,7 +207,8 @@ def train(net, feats, tgts, mask, epochs, batch=16, lr=1e-3, seed=0, log=print):
     return losses, time.time() - t0
 
 
-def time_to_image(net, plain_iters=30, seed=2001, device=0, windows=(1, 2), log=print):
+def time_to_image(net, plain_iters=30, seed=2001, device=0,
+                  rules=((tomo.LEARNED_MIN_DECREASE, tomo.LEARNED_PATIENCE),), log=print):
     """Plain weighted SIRT for plain_iters iterations vs the learned iteration to the same image error."""
     import torch
 
@@ -239,18 +240,19 @@ def time_to_image(net, plain_iters=30, seed=2001, device=0, windows=(1, 2), log=
         ctx.run_learned(net, sched, d_f.data_ptr(), d_fo.data_ptr(), -1.0, 1)   # warm up (illumination, graphs)
         out = {"plain_iters": plain_iters, "plain_seconds": t_plain, "plain_final_epsilon": target,
                "plain_epsilon": eps, "learned": {}}
-        for win in windows:
+        for rule in rules:
             d_f.zero_()
             torch.cuda.synchronize(dev)
-            leps, acc, t_learned = ctx.run_learned(net, sched, d_f.data_ptr(), d_fo.data_ptr(), target,
-                                                   3 * plain_iters, win)
+            leps, kind, sweeps, t_learned = ctx.run_learned(net, sched, d_f.data_ptr(), d_fo.data_ptr(), target,
+                                                            3 * plain_iters, *rule)
             leps = [float(e) for e in leps]
             reached = bool(leps[-1] <= target)
-            log(f"  learned (window {win}): {len(leps)} iterations ({int(acc.sum())} accepted), "
+            steps = "".join({1: "L", 0: "x", -1: "p"}[int(k)] for k in kind)
+            log(f"  learned (min decrease {rule[0]}, patience {rule[1]}): {steps}, {sweeps} sweeps, "
                 f"eps -> {leps[-1]:.3f} %, {t_learned:.3f} s, speedup "
                 f"{t_plain / t_learned if reached else float('nan'):.2f}")
-            out["learned"][str(win)] = {
-                "iters": len(leps), "accepted": [int(a) for a in acc], "seconds": t_learned,
+            out["learned"]["%g/%d" % rule] = {
+                "iters": len(leps), "steps": steps, "sweeps": sweeps, "seconds": t_learned,
                 "final_epsilon": leps[-1], "epsilon": leps, "reached": reached,
                 "speedup": t_plain / t_learned if reached else None}
     return out
@@ -314,7 +316,7 @@ def main():
     report["time_to_image"] = {}
     for seed in [int(x) for x in args.eval_seeds.split(",")]:
         print(f"  evaluation phantom seed {seed}")
-        report["time_to_image"][str(seed)] = time_to_image(net, seed=seed, windows=(1,))
+        report["time_to_image"][str(seed)] = time_to_image(net, seed=seed)
     print(json.dumps(report))
 
 

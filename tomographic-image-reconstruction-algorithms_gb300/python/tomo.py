@@ -34,6 +34,9 @@ METHOD_NAMES = {
 }
 # tomo_sched_kind
 SCHED_CONST, SCHED_POWER, SCHED_LINEAR = range(3)
+# acceptance rule of the learned step (tomo_run_learned): a proposal must lower the squared
+# record residual by 5 %; after 2 rejections in a row the run continues with plain steps
+LEARNED_MIN_DECREASE, LEARNED_PATIENCE = 0.05, 2
 
 
 class Config(C.Structure):
@@ -173,8 +176,8 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_net_train_step_device": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, DP]),
         "tomo_features_device": (i32, [vp, vp, vp, DP]),
         "tomo_iterate_learned": (i32, [vp, vp, C.POINTER(Schedule), i32, vp, vp, C.POINTER(IterStats), IP]),
-        "tomo_run_learned": (i32, [vp, vp, C.POINTER(Schedule), vp, vp, C.c_double, i32, i32, DP, IP, IP,
-                                   C.POINTER(C.c_double)]),
+        "tomo_run_learned": (i32, [vp, vp, C.POINTER(Schedule), vp, vp, C.c_double, i32, C.c_double, i32, DP, IP,
+                                   IP, IP, C.POINTER(C.c_double)]),
         "tomo_iterate_batch": (i32, [C.POINTER(vp), i32, i32, C.POINTER(Schedule), i32, i32, C.POINTER(vp),
                                      C.POINTER(vp), DP, C.POINTER(C.c_double)]),
     }
@@ -338,17 +341,20 @@ class Context:
         return stats, bool(acc.value)
 
     def run_learned(self, net: "Net", fallback: Schedule, d_f: int, d_ftrue: int = 0,
-                    target_eps: float = -1.0, max_iters: int = 50, window: int = 1):
+                    target_eps: float = -1.0, max_iters: int = 50, min_decrease: float = LEARNED_MIN_DECREASE,
+                    patience: int = LEARNED_PATIENCE):
         """Learned iterations on d_f until epsilon <= target_eps or max_iters:
-        (epsilon per iteration, accepted per iteration, wall seconds)."""
+        (epsilon per iteration, step kind per iteration [1 learned, 0 rejected, -1 plain],
+        gradient sweeps, wall seconds)."""
         eps = np.full(max(max_iters, 1), np.nan)
-        acc = np.zeros(max(max_iters, 1), np.int32)
-        done, secs = C.c_int32(), C.c_double()
+        kind = np.zeros(max(max_iters, 1), np.int32)
+        done, sweeps, secs = C.c_int32(), C.c_int32(), C.c_double()
         self._check(lib().tomo_run_learned(self.h, net.h, C.byref(fallback), C.c_void_p(d_f),
-                                           C.c_void_p(d_ftrue or None), target_eps, max_iters, window, _dp(eps),
-                                           _ip(acc), C.byref(done), C.byref(secs)))
+                                           C.c_void_p(d_ftrue or None), target_eps, max_iters, min_decrease,
+                                           patience, _dp(eps), _ip(kind), C.byref(done), C.byref(sweeps),
+                                           C.byref(secs)))
         n = done.value
-        return eps[:n], acc[:n].astype(bool), secs.value
+        return eps[:n], kind[:n], sweeps.value, secs.value
 
     @property
     def stream(self) -> int:
