@@ -128,7 +128,11 @@ typedef struct tomo_info {
 } tomo_info;
 
 typedef struct tomo_noise {
-    int32_t kind;            /* 0 none, 1 Gaussian rec += level*std(trace)*N(0,1) */
+    int32_t kind;            /* 0 none; 1 Gaussian rec += level*std(trace)*N(0,1);
+                                2, 3 multiplicative uniform: every record sample times
+                                1 + level*(2U - 1), U in [0,1) from a counter-based hash
+                                of (seed, group, step, channel) (the reference's
+                                0.9..1.1 factor of sirt-mimo-noise.cu:661-745 is level 0.1) */
     float level;
     uint64_t seed;
 } tomo_noise;
@@ -174,6 +178,14 @@ tomo_status tomo_forward(tomo_ctx* ctx, const float* f, float* records, float* u
 /* generate-data: forward solve plus optional seeded noise on the records. */
 tomo_status tomo_generate_data(tomo_ctx* ctx, const float* f_true, float* records,
                                const tomo_noise* noise);
+/* In-loop record noise for noise-robustness studies (sirt-mimo-noise.cu:661-745):
+ * every residual the context forms afterwards uses simulated samples times the
+ * multiplicative factor of `noise` (kind 2: a fresh draw for every gradient
+ * sweep, keyed by seed and the sweep count; kind 3: the same draw every sweep,
+ * equal to tomo_generate_data's kind-3 draw for the same seed, which is the
+ * reference's case of one factor shared by data and residual).  NULL or kind 0
+ * turns it off.  Captured graphs are rebuilt on the next call. */
+tomo_status tomo_set_residual_noise(tomo_ctx* ctx, const tomo_noise* noise);
 /* Store measured records on the device for later tomo_iterate calls. */
 tomo_status tomo_set_records(tomo_ctx* ctx, const float* records);
 /* Gradient of one SIRT sweep: forward, residual, time-reversed adjoint and

@@ -86,7 +86,25 @@ def test_cli_generate_field(built_lib, tmp_path):
     assert len(lines[0].split()) == 192 and lines[192] == ""
 
 
-def test_cli_usage_errors(built_lib, tmp_path):
-    exe = os.path.join(os.path.dirname(tomo.LIB_PATH), "..", "bin", "sirt-mimo-norm")
+@pytest.mark.parametrize("driver", ["sirt-mimo-norm", "sirt-mimo-seq", "sirt-mimo-norm-alt"])
+def test_cli_usage_errors(built_lib, tmp_path, driver):
+    exe = os.path.join(os.path.dirname(tomo.LIB_PATH), "..", "bin", driver)
     r = subprocess.run([exe, "fo.txt"], cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode == 1 and "Usage" in r.stderr
+
+
+def read_bin(path):
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"TOMOF32\n"
+    dims = np.frombuffer(raw[8:24], "<i4")
+    return dims, np.frombuffer(raw[24:], "<f4")
+
+
+def test_cli_generate_field_binary(built_lib, tmp_path):
+    """The binary form (magic, four int32 dims, float32 values) holds the same phantom."""
+    exe = os.path.join(os.path.dirname(tomo.LIB_PATH), "..", "bin", "generate-field")
+    r = subprocess.run([exe, "--binary"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    dims, vals = read_bin(tmp_path / "fo.bin")
+    assert list(dims) == [192, 192, 1, 1]
+    assert np.array_equal(vals.reshape(192, 192), O.phantom_ref())

@@ -237,6 +237,27 @@ def test_errors_are_status_codes():
         assert e.value.status == tomo.ERR_ARG
 
 
+@pytest.mark.parametrize("adj_rows", ["1004", "1108", "1216", "232"])
+def test_two_step_adjoint_variants_match_one_step(adj_rows, monkeypatch):
+    """The two-step adjoint's variants (interior fast path, inputs read ahead) give the one-step
+    kernel's bits on a grid wide enough to have interior strips (nx 256)."""
+    cfg0 = small_cfg(nx=256, ny=96, nt=161, n_transducers=32, radius=40.0, ckpt_interval=12)
+    fo = blob_phantom(96, 256, seed=18)
+    meas = O.forward(cfg0, fo.astype(np.float64))
+    f0 = blob_phantom(96, 256, seed=19, amp=0.01)
+    outs = []
+    for pair, rows in (("0", "4"), ("1", adj_rows)):
+        monkeypatch.setenv("TOMO_STRIP_ROWS", "4")
+        monkeypatch.setenv("TOMO_FWD_PAIR", "0")
+        monkeypatch.setenv("TOMO_ADJ_PAIR", pair)
+        monkeypatch.setenv("TOMO_ADJ_PAIR_ROWS", rows)
+        with tomo.Context(small_cfg(nx=256, ny=96, nt=161, n_transducers=32, radius=40.0, ckpt_interval=12)) as ctx:
+            dfg, _, r2 = ctx.gradient(f0, meas)
+        outs.append((dfg, r2))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert outs[0][1] == outs[1][1]
+
+
 @pytest.mark.parametrize("nt", [180, 181])
 def test_two_step_kernels_match_one_step(nt, monkeypatch):
     """Two time steps per launch (forward and adjoint) give the same bits as one."""

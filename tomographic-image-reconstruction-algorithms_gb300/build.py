@@ -40,6 +40,8 @@ DRIVERS = {
     "sirt-iter-norm": "SIRT_ITER_NORM",
     "art-mimo": "ART_MIMO",
     "art-mimo-io": "ART_MIMO_IO",
+    "sirt-mimo-seq": "SIRT_MIMO_SEQ",
+    "sirt-mimo-norm-alt": "SIRT_MIMO_NORM_ALT",
     "tomo": "TOMO_MULTI",
 }
 HEADERS = [os.path.join(INCLUDE, "tomo.h"), os.path.join(CSRC, "internal.h")]

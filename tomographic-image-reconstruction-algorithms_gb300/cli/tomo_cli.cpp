@@ -5,7 +5,9 @@
 // iteration.  Compiled once per driver with -DTOMO_DRIVER_<NAME>; the `tomo`
 // executable takes the driver name as its first argument.
 //
-//   generate-field                                  generate-field.cu:45-113
+//   generate-field [--binary]                       generate-field.cu:45-113
+// A phantom named *.bin selects the binary file form (cli/textio.h) for the
+// data files and the image a run writes; reading accepts either form.
 //   generate-data <fo> <gs> [<noise %>]              generate-data.cu:57-224
 //   sirt-mimo <gs> <eps> <iters> <omega>             sirt-mimo.cu:66-387
 //   sirt-mimo-io <fo> <gs> <eps> <iters> <w> <a> <b> <g>      sirt-mimo-io.cu
@@ -18,6 +20,11 @@
 //   sirt-iter-norm <fo> <gs> <eps> <iters> <w> <a>            sirt-iter-norm.cu
 //   art-mimo <gs> <eps> <iters> <omega>                       art-mimo.cu:480-788
 //   art-mimo-io <fo> <gs> <eps> <iters> <w> <a> <b> <g>       art-mimo-io.cu
+//   sirt-mimo-seq <fo> <gs> <eps> <iters> <w> <a> <b> <g>     sirt-mimo-seq.cu:34,337-596
+//       (5 ART iterations, then normalised SIRT; one schedule, iteration index continues)
+//   sirt-mimo-norm-alt <fo> <gs> <P> <eps> <iters> <a1> <b1> <n1> <a2> <b2> <n2>
+//       sirt-mimo-norm-alt.cu:126-156,421-477 (normalised SIRT, scale alternating between
+//       a1 + b1/k^n1 on odd and a2 - b2/k^n2 on even 1-based iterations k; a, b x 1000)
 // max iterations -1 means unbounded (sirt-mimo.cu:79-80).  Data files are
 // <base>-data-{bottom,right,top,left}-<gs>.txt (generate-data.cu:197-223).
 #include <algorithm>
@@ -26,6 +33,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <string>
 #include <vector>
@@ -64,15 +72,19 @@ bool parse_float(const char* s, float* out) {
     return true;
 }
 
-// "<base>.<ext>" with exactly one period (generate-data.cu:68-73)
+// Extension of every file a run writes: the phantom's (".txt", or ".bin" for the binary form).
+std::string g_ext = ".txt";
+
+// "<base>.<ext>" with exactly one period (generate-data.cu:68-73); sets the run's file form
 bool split_base(const std::string& fo, std::string* base) {
     if (std::count(fo.begin(), fo.end(), '.') != 1) return false;
     *base = fo.substr(0, fo.find('.'));
+    g_ext = textio::is_binary_name(fo) ? ".bin" : ".txt";
     return true;
 }
 
 std::string data_name(const std::string& base, int side, int gs) {
-    return base + "-data-" + kSides[side] + "-" + std::to_string(gs) + ".txt";
+    return base + "-data-" + kSides[side] + "-" + std::to_string(gs) + g_ext;
 }
 
 // records rec[g][k][side*nx + i]  <->  four files side[g][k][i]
@@ -160,6 +172,9 @@ struct LoopOpts {
     bool abs_threshold;      // |file_eps - eps| > 0.2 (norm) vs file_eps - eps > 0.2 (classic)
     const char* conv_name;   // sirt_convergence.txt / art_convergence.txt
     const char* time_name;
+    // optional per-iteration method and schedule (hybrid and alternating drivers)
+    std::function<int(int)> method_at;
+    std::function<tomo_schedule(int)> sched_at;
 };
 
 // The iteration loop with the reference's stopping rule and log files.
@@ -176,7 +191,9 @@ int iterate_loop(Problem& p, const LoopOpts& o, std::vector<float>& f) {
     int rc = 0;
     for (int64_t it = 0; it < limit; ++it) {
         tomo_iter_stats st{};
-        if (check(tomo_iterate(p.ctx, o.method, &o.sched, (int)it, f.data(), nullptr, p.fo.data(), &st), p.ctx,
+        const int method = o.method_at ? o.method_at((int)it) : o.method;
+        const tomo_schedule sc = o.sched_at ? o.sched_at((int)it) : o.sched;
+        if (check(tomo_iterate(p.ctx, method, &sc, (int)it, f.data(), nullptr, p.fo.data(), &st), p.ctx,
                   "tomo_iterate")) { rc = 1; break; }
         const float eps = (float)st.epsilon;
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -217,14 +234,15 @@ void usage(const char* prog, const char* args) { std::fprintf(stderr, "Usage: %s
 
 // ---------------------------------------------------------------------------
 int cmd_generate_field(int argc, char** argv) {
-    (void)argv;
-    if (argc != 1) { usage(argv[0], ""); return 1; }
+    const bool binary = argc == 2 && std::strcmp(argv[1], "--binary") == 0;
+    if (argc != 1 && !binary) { usage(argv[0], "[--binary]"); return 1; }
     tomo_config cfg;
     tomo_config_init(&cfg, TOMO_PROFILE_REF);
     std::vector<float> fo((size_t)cfg.nx * cfg.ny);
     if (check(tomo_phantom_ref(cfg.nx, cfg.ny, fo.data()), nullptr, "tomo_phantom_ref")) return 1;
-    std::fprintf(stderr, "writing to 'fo.txt'...\n\n");
-    return textio::write_floats("fo.txt", fo.data(), cfg.nx, cfg.ny) ? 0 : die("cannot write fo.txt");
+    const char* name = binary ? "fo.bin" : "fo.txt";
+    std::fprintf(stderr, "writing to '%s'...\n\n", name);
+    return textio::write_floats(name, fo.data(), cfg.nx, cfg.ny) ? 0 : die("cannot write the phantom");
 }
 
 int cmd_generate_data(int argc, char** argv) {
@@ -317,7 +335,62 @@ int cmd_io(int argc, char** argv, int method, const char* prefix, int variant) {
                art ? "art_convergence.txt" : "sirt_convergence.txt", art ? "art_time.txt" : "sirt_time.txt"};
     std::vector<float> f;
     if (iterate_loop(p, o, f)) return 1;
-    const std::string name = std::string(prefix) + std::to_string(gs) + "-" + base + ".txt";
+    const std::string name = std::string(prefix) + std::to_string(gs) + "-" + base + g_ext;
+    return textio::write_floats(name, f.data(), p.cfg.nx, p.cfg.ny) ? 0 : die("cannot write image");
+}
+
+// sirt-mimo-seq: INITIAL_ITERATIONS = 5 ART iterations, then normalised SIRT.
+int cmd_seq(int argc, char** argv) {
+    if (argc != 9) {
+        usage(argv[0], "<fo_filename> <sensor group size> <target epsilon> <max iterations> <omega> <alpha> <beta> <gamma>");
+        return 1;
+    }
+    int gs, iters;
+    float target, w, al, be, ga;
+    if (!parse_int(argv[2], &gs) || !parse_float(argv[3], &target) || !parse_int(argv[4], &iters) ||
+        !parse_float(argv[5], &w) || !parse_float(argv[6], &al) || !parse_float(argv[7], &be) ||
+        !parse_float(argv[8], &ga))
+        return die("bad arguments");
+    Problem p;
+    std::string base;
+    if (open_problem(p, gs, 0) || load_inputs(p, argv[1], gs, &base)) return 1;   // ART passes one group at a time
+    LoopOpts o{TOMO_SIRT_NORM, sched(TOMO_SCHED_POWER, w, al, be, ga), target, iters, true, true,
+               "sirt_convergence.txt", "sirt_time.txt", nullptr, nullptr};
+    o.method_at = [](int it) { return it < 5 ? TOMO_ART : TOMO_SIRT_NORM; };
+    std::vector<float> f;
+    if (iterate_loop(p, o, f)) return 1;
+    const std::string name = "sirt-norm-" + std::to_string(gs) + "-" + base + g_ext;
+    return textio::write_floats(name, f.data(), p.cfg.nx, p.cfg.ny) ? 0 : die("cannot write image");
+}
+
+// sirt-mimo-norm-alt: normalised SIRT with the alternating relaxation scale.
+int cmd_norm_alt(int argc, char** argv) {
+    if (argc != 12) {
+        usage(argv[0], "<fo_filename> <group size> <parallel groups> <target epsilon> <max iterations> <alpha1> "
+                       "<beta1> <n1> <alpha2> <beta2> <n2>");
+        return 1;
+    }
+    int gs, P, iters;
+    float target, a1, b1, n1, a2, b2, n2;
+    if (!parse_int(argv[2], &gs) || !parse_int(argv[3], &P) || !parse_float(argv[4], &target) ||
+        !parse_int(argv[5], &iters) || !parse_float(argv[6], &a1) || !parse_float(argv[7], &b1) ||
+        !parse_float(argv[8], &n1) || !parse_float(argv[9], &a2) || !parse_float(argv[10], &b2) ||
+        !parse_float(argv[11], &n2))
+        return die("bad arguments");
+    a1 *= 1000.f; b1 *= 1000.f; a2 *= 1000.f; b2 *= 1000.f;     // sirt-mimo-norm-alt.cu:143-148
+    Problem p;
+    std::string base;
+    if (open_problem(p, gs, P) || load_inputs(p, argv[1], gs, &base)) return 1;
+    LoopOpts o{TOMO_SIRT_NORM, sched(TOMO_SCHED_CONST, 1.f, 0, 0, 1), target, iters, true, true,
+               "sirt_convergence.txt", "sirt_time.txt", nullptr, nullptr};
+    o.sched_at = [=](int it) {
+        const int k = it + 1;                                   // the reference counts from 1
+        const float scale = k % 2 != 0 ? a1 + b1 / std::pow((float)k, n1) : a2 - b2 / std::pow((float)k, n2);
+        return sched(TOMO_SCHED_CONST, scale, 0, 0, 1);
+    };
+    std::vector<float> f;
+    if (iterate_loop(p, o, f)) return 1;
+    const std::string name = "sirt-norm-" + std::to_string(gs) + "-" + base + g_ext;
     return textio::write_floats(name, f.data(), p.cfg.nx, p.cfg.ny) ? 0 : die("cannot write image");
 }
 
@@ -335,6 +408,8 @@ int dispatch(const std::string& name, int argc, char** argv) {
     if (name == "sirt-iter") return cmd_io(argc, argv, TOMO_SIRT_SCALED, "sirt-", 4);
     if (name == "sirt-iter-norm") return cmd_io(argc, argv, TOMO_SIRT_NORM, "sirt-norm-", 5);
     if (name == "art-mimo-io") return cmd_io(argc, argv, TOMO_ART, "art-", 0);
+    if (name == "sirt-mimo-seq") return cmd_seq(argc, argv);
+    if (name == "sirt-mimo-norm-alt") return cmd_norm_alt(argc, argv);
     std::fprintf(stderr, "unknown driver '%s'\n", name.c_str());
     return 2;
 }
@@ -376,6 +451,10 @@ int main(int argc, char** argv) {
         "art-mimo";
 #elif defined(TOMO_DRIVER_ART_MIMO_IO)
         "art-mimo-io";
+#elif defined(TOMO_DRIVER_SIRT_MIMO_SEQ)
+        "sirt-mimo-seq";
+#elif defined(TOMO_DRIVER_SIRT_MIMO_NORM_ALT)
+        "sirt-mimo-norm-alt";
 #else
         "unknown";
 #endif

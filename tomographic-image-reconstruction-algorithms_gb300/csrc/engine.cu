@@ -112,6 +112,16 @@ struct tomo_ctx {
         *p = (T*)q;
         return TOMO_OK;
     }
+    // residual noise (tomo_set_residual_noise): kind 0 off, 2 a fresh draw per gradient sweep,
+    // 3 one fixed draw; the key lives on the device so captured graphs see its updates
+    int noise_kind = 0;
+    uint64_t noise_seed = 0, noise_draws = 0, noise_key_host = 0;
+    uint64_t* noise_key = nullptr;
+    void drop_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+        graph_kernels.clear();
+    }
     ~tomo_ctx() {
         if (dev >= 0) cudaSetDevice(dev);
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -281,7 +291,8 @@ tomo_status autotune(tomo_ctx* c) {
             }
             if (ms < best_f) { best_f = ms; c->rows_fwd2 = code; c->fwd_pair = true; }
         }
-        for (int code : {rows, 100 + rows, 200 + rows}) {   // two steps per launch: reps/2 launches cover the same steps
+        // two steps per launch (reps/2 launches cover the same steps); codes as launch_adj2_strip
+        for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows}) {
             if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {
@@ -477,6 +488,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         }
         fwd_launch(c, fs);
         GatherStep gs{};
+        gs.g0 = g0;
         gs.u = c->hist + c->slot(m);
         gs.gstride = gstride;
         gs.k = m;
@@ -491,6 +503,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     if (c->strip) {
         for (int m = std::max(gnext, 2); m < nt - 1; ++m) {   // slices left before the last
             GatherStep gs{};
+            gs.g0 = g0;
             gs.u = c->hist + c->slot(m);
             gs.gstride = gstride;
             gs.k = m;
@@ -503,6 +516,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     }
     if (c->strip) {
         GatherStep gs{};
+        gs.g0 = g0;
         gs.u = c->hist + c->slot(nt - 1);
         gs.gstride = gstride;
         gs.k = nt - 1;
@@ -611,8 +625,20 @@ tomo_status forward_all(tomo_ctx* c, float* u_last_host) {
     return TOMO_OK;
 }
 
+// Noise key of the next residual sweep (kind 2: a new draw each sweep).
+tomo_status next_noise_draw(tomo_ctx* c) {
+    if (c->noise_kind != 2) return TOMO_OK;
+    uint64_t z = c->noise_seed + 0x9E3779B97F4A7C15ull * (++c->noise_draws);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    c->noise_key_host = z ^ (z >> 31);
+    CU(c, cudaMemcpyAsync(c->noise_key, &c->noise_key_host, sizeof(uint64_t), cudaMemcpyHostToDevice, c->st));
+    return TOMO_OK;
+}
+
 // Correlations of all groups for the current c->f (SIRT), residual partials.
 tomo_status gradient_all(tomo_ctx* c) {
+    TRY(next_noise_draw(c));
     const Geometry& g = c->geo;
     launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
     ++c->launches;
@@ -680,6 +706,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
     if (method == TOMO_ART) {
         // art-mimo.cu:688-736: each group sees the field updated by the previous one.
         double acc = 0.0;
+        TRY(next_noise_draw(c));
         for (int gg = 0; gg < G; ++gg) {
             launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
             TRY(run_pass(c, MODE_GRAD, gg, 1));
@@ -943,8 +970,32 @@ tomo_status tomo_generate_data(tomo_ctx* c, const float* f_true, float* records,
     TRY(tomo_forward(c, f_true, records, nullptr));
     if (noise && noise->kind == 1 && noise->level > 0.f)
         add_record_noise(records, c->geo.G, c->geo.nt, c->geo.nch, noise->level, noise->seed);
-    else if (noise && noise->kind != 0 && noise->kind != 1)
+    else if (noise && (noise->kind == 2 || noise->kind == 3) && noise->level > 0.f)
+        mul_record_noise(records, c->geo.G, c->geo.nt, c->geo.nch, noise->level, noise->seed);
+    else if (noise && (noise->kind < 0 || noise->kind > 3))
         return c->fail(TOMO_ERR_ARG, "unknown noise kind %d", noise->kind);
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_residual_noise(tomo_ctx* c, const tomo_noise* noise) {
+    if (!c) return TOMO_ERR_ARG;
+    const int kind = noise ? noise->kind : 0;
+    if (kind != 0 && kind != 2 && kind != 3) return c->fail(TOMO_ERR_ARG, "residual noise kind must be 0, 2 or 3");
+    if (noise && kind != 0 && !(noise->level >= 0.f && noise->level < 1.f))
+        return c->fail(TOMO_ERR_ARG, "residual noise level must be in [0, 1)");
+    CU(c, cudaSetDevice(c->dev));
+    if (kind != 0 && !c->noise_key) TRY(c->alloc(&c->noise_key, 1, "noise key"));
+    CU(c, cudaStreamSynchronize(c->st));
+    c->noise_kind = kind;
+    c->noise_seed = noise ? noise->seed : 0;
+    c->noise_draws = 0;
+    c->noise_key_host = c->noise_seed;
+    if (kind != 0)
+        CU(c, cudaMemcpyAsync(c->noise_key, &c->noise_key_host, sizeof(uint64_t), cudaMemcpyHostToDevice, c->st));
+    c->dg.noise_key = kind != 0 ? c->noise_key : nullptr;
+    c->dg.noise_level = kind != 0 ? noise->level : 0.f;
+    c->drop_graphs();                       // captured launches hold the old DevGeo
+    CU(c, cudaStreamSynchronize(c->st));
     return TOMO_OK;
 }
 
@@ -1095,6 +1146,7 @@ tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule
     launch_apply(c->f, c->dnet, c->mask, N, 1.0, nullptr, c->st);
     launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
     c->launches += 2;
+    TRY(next_noise_draw(c));
     for (int g0 = 0; g0 < g.G; g0 += c->P) TRY(run_pass(c, MODE_RESID, g0, std::min(c->P, g.G - g0)));
     TRY(residual_norm(c, &r1));
     const bool ok = r1 < r0;

@@ -254,6 +254,12 @@ void add_record_noise(float* rec, int G, int nt, int nch, float level, uint64_t 
         }
 }
 
+void mul_record_noise(float* rec, int G, int nt, int nch, float level, uint64_t seed) {
+    for (int g = 0; g < G; ++g)
+        for (int k = 0; k < nt; ++k)
+            for (int c = 0; c < nch; ++c) rec[((int64_t)g * nt + k) * nch + c] *= noise_factor(seed, level, g, k, c);
+}
+
 void fill_damp(DevGeo& g) {
     for (int dd = 0; dd < 64; ++dd) {
         const double x = dd < g.sponge_w ? (double)(g.sponge_w - dd) / (double)g.sponge_w : 0.0;

@@ -7,7 +7,29 @@
 
 #include "tomo.h"
 
+#ifdef __CUDACC__
+#define TOMO_HD __host__ __device__
+#else
+#define TOMO_HD
+#endif
+
 namespace tomo {
+
+// Counter-based uniform draw in [0, 1) for record sample (group g, step k, channel c) under
+// `key` (a splitmix64 finaliser of the mixed indices; the same bits on host and device).
+TOMO_HD inline float noise_uniform(uint64_t key, int g, int k, int c) {
+    uint64_t z = key ^ ((uint64_t)(uint32_t)g << 42) ^ ((uint64_t)(uint32_t)k << 20) ^ (uint64_t)(uint32_t)c;
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (float)(z >> 40) * (1.0f / 16777216.0f);
+}
+
+// Multiplicative record noise factor 1 + level (2U - 1).
+TOMO_HD inline float noise_factor(uint64_t key, float level, int g, int k, int c) {
+    return 1.0f + level * (2.0f * noise_uniform(key, g, k, c) - 1.0f);
+}
 
 // Reference constants (sirt-mimo.cu:26-35), the float values the reference uses.
 constexpr float kRefH = 0.001f;
@@ -45,6 +67,8 @@ tomo_status phantom_cfg(int nx, int ny, int kind, int n, float rmin, float rmax,
                         float noise_sigma, float support, uint64_t seed, float* fo);
 // rec += level * std(trace) * N(0,1) per (group, channel) trace, seeded.
 void add_record_noise(float* rec, int G, int nt, int nch, float level, uint64_t seed);
+// rec *= noise_factor(seed, level, g, k, c) for every sample (multiplicative uniform noise).
+void mul_record_noise(float* rec, int G, int nt, int nch, float level, uint64_t seed);
 
 // splitmix64-based portable RNG (identical on x86 and Arm).
 struct Rng {
@@ -76,6 +100,10 @@ struct DevGeo {
     int rwords;            // words of rbits per row
     const float* src;      // per step source factor
     int n_src_steps;
+    // residual noise: simulated samples u become u * noise_factor(*noise_key, noise_level, ...)
+    // in every residual gather while noise_key is non-null (its value can change between passes)
+    const uint64_t* noise_key;
+    float noise_level;
 };
 
 struct FwdStep {
@@ -117,6 +145,7 @@ struct GatherStep {
     double* part;        // per (group, k) squared residual, pass-group 0, stride nt; or null
     int k;
     int ng;
+    int g0 = 0;          // global index of pass-group 0
 };
 
 // ---- kernel launchers (kernels.cu) --------------------------------------------------

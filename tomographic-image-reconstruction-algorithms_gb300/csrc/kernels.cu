@@ -208,10 +208,13 @@ __global__ void __launch_bounds__(256) k_gather(DevGeo g, GatherStep s) {
     const int gl = blockIdx.x;
     const float* u = s.u + gl * s.gstride;
     const int64_t base = ((int64_t)gl * g.nt + s.k) * g.nch;
+    const bool noisy = s.meas && g.noise_key;
+    const uint64_t key = noisy ? *g.noise_key : 0;
     double acc = 0.0;
     for (int c = threadIdx.x; c < g.nch; c += blockDim.x) {
         const int cell = g.rcv[c];
-        const float v = cell >= 0 ? u[cell] : 0.f;
+        float v = cell >= 0 ? u[cell] : 0.f;
+        if (noisy) v *= noise_factor(key, g.noise_level, s.g0 + gl, s.k, c);
         if (s.meas) {
             const float e = cell >= 0 ? s.meas[base + c] - v : 0.f;
             s.out[base + c] = e;

@@ -138,9 +138,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_fwd_strip(DevGeo g, const float*
         if (blockIdx.x != 0 || s.gk < 2) return;
         const float* u = s.uc + gl * s.gstride;
         const int64_t base = ((int64_t)gl * g.nt + s.gk) * g.nch;
+        const bool noisy = s.gmeas && g.noise_key;
+        const uint64_t key = noisy ? *g.noise_key : 0;
         for (int c = threadIdx.x; c < g.nch; c += blockDim.x) {
             const int cell = g.rcv[c];
-            const float v = cell >= 0 ? u[cell] : 0.f;
+            float v = cell >= 0 ? u[cell] : 0.f;
+            if (noisy) v *= noise_factor(key, g.noise_level, s.g0 + gl, s.gk, c);
             s.gout[base + c] = s.gmeas ? (cell >= 0 ? s.gmeas[base + c] - v : 0.f) : v;
         }
         return;
@@ -335,21 +338,17 @@ __device__ __forceinline__ float2 ld2(const float* __restrict__ p, int64_t off, 
     return ok ? *reinterpret_cast<const float2*>(p + off) : make_float2(0.f, 0.f);
 }
 
-// AHEAD: 0 reads each row's inputs in the iteration that uses them; 1 also reads the
-// correlation row one iteration ahead; 2 reads every input one iteration ahead (more loads in
-// flight per warp, more registers: 8 / 7 / 5 blocks per SM).
-template <int R, int AHEAD>
-__global__ void __launch_bounds__(WARPS * 32, AHEAD == 2 ? 5 : 8 - AHEAD) k_adj2_strip(DevGeo g, const float* __restrict__ coef,
-                                                                     Adj2Step s) {
+// Rows y0 .. y0+R-1 of one warp strip.  EDGE = false: the strip, its one-cell halo and rows
+// y0-2 .. y0+R+2 lie inside the grid, so no access needs a bounds predicate.
+template <int R, int AHEAD, bool EDGE>
+__device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restrict__ coef, const Adj2Step& s,
+                                          int x0, int y0) {
     constexpr bool PF = AHEAD >= 1;
     const int nx = g.nx, ny = g.ny;
     const int gl = blockIdx.z;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int x0 = blockIdx.x * 60 - 2;
+    const int lane = threadIdx.x & 31;
     const int i = x0 + 2 * lane;
-    const int y0 = (blockIdx.y * WARPS + warp) * R;
-    if (y0 >= ny) return;
-    const bool in = i >= 0 && i < nx;
+    const bool in = !EDGE || (i >= 0 && i < nx);
     const bool own = in && lane >= 1 && lane <= 30;
     const int yend = min(y0 + R, ny);          // rows y0 .. yend-1 are written
     const float* z1 = s.z1 + gl * s.zstride;
@@ -362,7 +361,7 @@ __global__ void __launch_bounds__(WARPS * 32, AHEAD == 2 ? 5 : 8 - AHEAD) k_adj2
     const float* rrb = s.rrb + gl * s.rrstride;
     float* corr = s.corr + gl * s.cstride;
     const bool edge_x = x0 < g.sponge_w || x0 + 64 > nx - g.sponge_w;
-    auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
+    auto row_ok = [&](int r) { return !EDGE || (in && r >= 0 && r < ny); };
     const RcvMask rk = rcv_mask(g, x0, x0 + 64);
     const int dca = edge_dist(i, nx), dcb = edge_dist(i + 1, nx);
     // rolling state at the top of iteration r (first step at row r, second at row r-1), with
@@ -396,7 +395,7 @@ __global__ void __launch_bounds__(WARPS * 32, AHEAD == 2 ? 5 : 8 - AHEAD) k_adj2
     }
 #pragma unroll 1
     for (int r = y0 - 1; r <= y0 + R; ++r) {
-        if (r > ny) break;
+        if (EDGE && r > ny) break;
         const int row = r * nx;
         const bool ok = row_ok(r);
         float2 z1p, cp, zz, ua0, ub0;
@@ -486,11 +485,33 @@ __global__ void __launch_bounds__(WARPS * 32, AHEAD == 2 ? 5 : 8 - AHEAD) k_adj2
     }
 }
 
-template <int R, int AHEAD>
+// AHEAD: 0 reads each row's inputs in the iteration that uses them; 1 also reads the
+// correlation row one iteration ahead; 2 reads every input one iteration ahead (more loads in
+// flight per warp).  SPLIT: warps whose strip lies inside the grid take a path without bounds
+// predicates (the compiler then overlaps more loads, at more registers).  Minimum resident
+// blocks per SM: 8 / 7 / 5 (AHEAD 0 / 1 / 2), 6 / 5 / 4 with SPLIT.
+constexpr int adj2_min_blocks(int ahead, bool split) {
+    return split ? (ahead == 2 ? 4 : 6 - ahead) : (ahead == 2 ? 5 : 8 - ahead);
+}
+
+template <int R, int AHEAD, bool SPLIT>
+__global__ void __launch_bounds__(WARPS * 32, adj2_min_blocks(AHEAD, SPLIT))
+    k_adj2_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
+    const int warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 60 - 2;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= g.ny) return;
+    if (SPLIT && x0 > 0 && x0 + 64 < g.nx && y0 >= 2 && y0 + R + 2 < g.ny)
+        adj2_rows<R, AHEAD, false>(g, coef, s, x0, y0);
+    else
+        adj2_rows<R, AHEAD, true>(g, coef, s, x0, y0);
+}
+
+template <int R, int AHEAD, bool SPLIT>
 void adj2_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     dim3 grid((g.nx + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
-    k_adj2_strip<R, AHEAD><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+    k_adj2_strip<R, AHEAD, SPLIT><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -515,12 +536,15 @@ struct Fwd2Step {
     float* gout;
 };
 
-__device__ __forceinline__ void gather_slice(const DevGeo& g, const float* u, int gl, int gk, const float* gmeas,
-                                             float* gout) {
+__device__ __forceinline__ void gather_slice(const DevGeo& g, const float* u, int gl, int g0, int gk,
+                                             const float* gmeas, float* gout) {
     const int64_t base = ((int64_t)gl * g.nt + gk) * g.nch;
+    const bool noisy = gmeas && g.noise_key;
+    const uint64_t key = noisy ? *g.noise_key : 0;
     for (int c = threadIdx.x; c < g.nch; c += blockDim.x) {
         const int cell = g.rcv[c];
-        const float v = cell >= 0 ? u[cell] : 0.f;
+        float v = cell >= 0 ? u[cell] : 0.f;
+        if (noisy) v *= noise_factor(key, g.noise_level, g0 + gl, gk, c);
         gout[base + c] = gmeas ? (cell >= 0 ? gmeas[base + c] - v : 0.f) : v;
     }
 }
@@ -531,8 +555,8 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_fwd2_strip(DevGeo g, const fl
     const int gl = blockIdx.z;
     if (blockIdx.y == gridDim.y - 1) {
         if (blockIdx.x != 0) return;
-        if (s.gka >= 2) gather_slice(g, s.up + gl * s.gstride, gl, s.gka, s.gmeas, s.gout);
-        if (s.gkb >= 2) gather_slice(g, s.uc + gl * s.gstride, gl, s.gkb, s.gmeas, s.gout);
+        if (s.gka >= 2) gather_slice(g, s.up + gl * s.gstride, gl, s.g0, s.gka, s.gmeas, s.gout);
+        if (s.gkb >= 2) gather_slice(g, s.uc + gl * s.gstride, gl, s.g0, s.gkb, s.gmeas, s.gout);
         return;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -622,8 +646,8 @@ __global__ void __launch_bounds__(WARPS * 32, 6) k_fwd2q_strip(DevGeo g, const f
     const int gl = blockIdx.z;
     if (blockIdx.y == gridDim.y - 1) {
         if (blockIdx.x != 0) return;
-        if (s.gka >= 2) gather_slice(g, s.up + gl * s.gstride, gl, s.gka, s.gmeas, s.gout);
-        if (s.gkb >= 2) gather_slice(g, s.uc + gl * s.gstride, gl, s.gkb, s.gmeas, s.gout);
+        if (s.gka >= 2) gather_slice(g, s.up + gl * s.gstride, gl, s.g0, s.gka, s.gmeas, s.gout);
+        if (s.gkb >= 2) gather_slice(g, s.uc + gl * s.gstride, gl, s.g0, s.gkb, s.gmeas, s.gout);
         return;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -767,20 +791,17 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     s.rra = a.rr; s.rrb = b.rr; s.rrstride = a.rrstride;
     s.corr = a.corr; s.cstride = a.cstride; s.ng = a.ng;
     cudaStream_t st = (cudaStream_t)stream;
-    switch (rows) {   // rows + 100 * AHEAD (inputs read one iteration ahead, see k_adj2_strip)
-    case 4: adj2_strip<4, 0>(g, coef, s, st); break;
-    case 16: adj2_strip<16, 0>(g, coef, s, st); break;
-    case 32: adj2_strip<32, 0>(g, coef, s, st); break;
-    case 104: adj2_strip<4, 1>(g, coef, s, st); break;
-    case 108: adj2_strip<8, 1>(g, coef, s, st); break;
-    case 116: adj2_strip<16, 1>(g, coef, s, st); break;
-    case 132: adj2_strip<32, 1>(g, coef, s, st); break;
-    case 204: adj2_strip<4, 2>(g, coef, s, st); break;
-    case 208: adj2_strip<8, 2>(g, coef, s, st); break;
-    case 216: adj2_strip<16, 2>(g, coef, s, st); break;
-    case 232: adj2_strip<32, 2>(g, coef, s, st); break;
-    default: adj2_strip<8, 0>(g, coef, s, st); break;
+    // code = rows + 100 * AHEAD + 1000 * SPLIT (see k_adj2_strip)
+#define ADJ2_CASE(R, A, S) \
+    case (R) + 100 * (A) + 1000 * (S): adj2_strip<R, A, S>(g, coef, s, st); return;
+#define ADJ2_ROWS(A, S) ADJ2_CASE(4, A, S) ADJ2_CASE(8, A, S) ADJ2_CASE(16, A, S) ADJ2_CASE(32, A, S)
+    switch (rows) {
+        ADJ2_ROWS(0, false) ADJ2_ROWS(1, false) ADJ2_ROWS(2, false)
+        ADJ2_ROWS(0, true) ADJ2_ROWS(1, true) ADJ2_ROWS(2, true)
+    default: adj2_strip<8, 0, false>(g, coef, s, st); return;
     }
+#undef ADJ2_ROWS
+#undef ADJ2_CASE
 }
 
 void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& s, void* stream) {

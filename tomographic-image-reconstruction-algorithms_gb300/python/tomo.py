@@ -155,6 +155,7 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_forward": (i32, [vp, FP, FP, FP]),
         "tomo_generate_data": (i32, [vp, FP, FP, C.POINTER(Noise)]),
         "tomo_set_records": (i32, [vp, FP]),
+        "tomo_set_residual_noise": (i32, [vp, C.POINTER(Noise)]),
         "tomo_gradient": (i32, [vp, FP, FP, FP, FP, DP]),
         "tomo_iterate": (i32, [vp, i32, C.POINTER(Schedule), i32, FP, FP, FP, C.POINTER(IterStats)]),
         "tomo_run": (i32, [vp, i32, C.POINTER(Schedule), FP, FP, FP, f32, i32, DP, IP]),
@@ -265,12 +266,18 @@ class Context:
         self._check(lib().tomo_forward(self.h, _fp(f), _fp(rec), _fp(ul)))
         return (rec, ul) if u_last else rec
 
-    def generate_data(self, f_true, noise_level=0.0, seed=0):
+    def generate_data(self, f_true, noise_level=0.0, seed=0, kind=1):
+        """Forward records plus seeded noise (kind 1 additive Gaussian, 2/3 multiplicative uniform)."""
         f = np.ascontiguousarray(f_true, np.float32)
         rec = np.zeros(self.records_shape(), np.float32)
-        nz = Noise(kind=1 if noise_level > 0 else 0, level=noise_level, seed=seed)
+        nz = Noise(kind=kind if noise_level > 0 else 0, level=noise_level, seed=seed)
         self._check(lib().tomo_generate_data(self.h, _fp(f), _fp(rec), C.byref(nz)))
         return rec
+
+    def set_residual_noise(self, kind=0, level=0.0, seed=0):
+        """In-loop multiplicative record noise (kind 2 fresh per sweep, 3 fixed; 0 off)."""
+        nz = Noise(kind=kind, level=level, seed=seed)
+        self._check(lib().tomo_set_residual_noise(self.h, C.byref(nz)))
 
     def set_records(self, rec):
         rec = np.ascontiguousarray(rec, np.float32)
