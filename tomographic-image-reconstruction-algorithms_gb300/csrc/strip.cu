@@ -380,10 +380,12 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
     float2 ubm2 = make_float2(0.f, 0.f), ubm = make_float2(0.f, 0.f);
     float2 crm = make_float2(0.f, 0.f);
     int2 ridm = make_int2(-1, -1);
+    bool rcvm = false;                         // row r-1 has receivers in the strip
     // AHEAD == 2: the inputs of the coming iteration (rows r+1 of z(kz+1) and the coefficient,
     // rows r of z(kz+2), u(q), u(q-1) and the receiver ids)
     float2 q_z1 = make_float2(0.f, 0.f), q_c = q_z1, q_zz = q_z1, q_ua = q_z1, q_ub = q_z1;
     int2 q_rid = make_int2(-1, -1);
+    bool q_rcv = false;
     if (AHEAD == 2) {
         const int r = y0 - 1, row = r * nx;
         q_z1 = ld2(z1, row + nx + i, row_ok(r + 1));
@@ -391,7 +393,8 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
         q_zz = ld2(z2, row + i, row_ok(r));
         q_ua = ld2(ua, row + i, row_ok(r));
         q_ub = ld2(ub, row + i, row_ok(r));
-        if (rcv_row(g, rk, r) && row_ok(r)) q_rid = *reinterpret_cast<const int2*>(g.rid + row + i);
+        q_rcv = rcv_row(g, rk, r);
+        if (q_rcv && row_ok(r)) q_rid = *reinterpret_cast<const int2*>(g.rid + row + i);
     }
 #pragma unroll 1
     for (int r = y0 - 1; r <= y0 + R; ++r) {
@@ -400,8 +403,9 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
         const bool ok = row_ok(r);
         float2 z1p, cp, zz, ua0, ub0;
         int2 rid = make_int2(-1, -1);
+        bool rcv;
         if (AHEAD == 2) {
-            z1p = q_z1; cp = q_c; zz = q_zz; ua0 = q_ua; ub0 = q_ub; rid = q_rid;
+            z1p = q_z1; cp = q_c; zz = q_zz; ua0 = q_ua; ub0 = q_ub; rid = q_rid; rcv = q_rcv;
             const int rn = r + 1, rown = row + nx;
             q_z1 = ld2(z1, rown + nx + i, row_ok(rn + 1));
             q_c = ld2(coef, rown + nx + i, row_ok(rn + 1));
@@ -409,7 +413,8 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
             q_ua = ld2(ua, rown + i, row_ok(rn));
             q_ub = ld2(ub, rown + i, row_ok(rn));
             q_rid = make_int2(-1, -1);
-            if (rcv_row(g, rk, rn) && row_ok(rn)) q_rid = *reinterpret_cast<const int2*>(g.rid + rown + i);
+            q_rcv = rcv_row(g, rk, rn);
+            if (q_rcv && row_ok(rn)) q_rid = *reinterpret_cast<const int2*>(g.rid + rown + i);
         } else {
             const bool okn = row_ok(r + 1);
             z1p = ld2(z1, row + nx + i, okn);
@@ -417,7 +422,8 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
             zz = ld2(z2, row + i, ok);
             ua0 = ld2(ua, row + i, ok);
             ub0 = ld2(ub, row + i, ok);
-            if (rcv_row(g, rk, r) && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
+            rcv = rcv_row(g, rk, r);
+            if (rcv && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
         }
         // correlation of row r, read now for the second step of the next iteration
         float2 cr_next = make_float2(0.f, 0.f);
@@ -426,16 +432,19 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
         // ---- first step: z(kz) at row r (all lanes; zero outside the grid)
         float2 za0 = make_float2(0.f, 0.f);
         {
-            float pw = __shfl_up_sync(FULL, pz0.y, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
-            if (lane == 0) pw = (ok && x0 > 0) ? mul(coef[row + x0 - 1], z1[row + x0 - 1]) : 0.f;
-            if (lane == 31) pe = (ok && x0 + 64 < nx) ? mul(coef[row + x0 + 64], z1[row + x0 + 64]) : 0.f;
+            // lane 0's west and lane 31's east neighbour come from no lane: only the halo cells
+            // x0 and x0+63, whose first-step values no owned cell reads, would use them
+            const float pw = __shfl_up_sync(FULL, pz0.y, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
             if (ok) {
-                const bool near = edge_x || r < g.sponge_w || r >= ny - g.sponge_w;
                 const int dr = edge_dist(r, ny);
-                const float ix = rid.x >= 0 ? rra[rid.x] : 0.f;
-                const float iy = rid.y >= 0 ? rra[rid.y] : 0.f;
-                const float dx = near ? damp_at(g, dca, dr) : 1.f;
-                const float dy = near ? damp_at(g, dcb, dr) : 1.f;
+                const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+                float dx = drow, dy = drow;
+                if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+                float ix = 0.f, iy = 0.f;
+                if (rcv) {
+                    ix = rid.x >= 0 ? rra[rid.x] : 0.f;
+                    iy = rid.y >= 0 ? rra[rid.y] : 0.f;
+                }
                 za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, ix, dx);
                 za0.y = adj_cell(pe, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, iy, dy);
             }
@@ -449,13 +458,16 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
             const float uaw = __shfl_up_sync(FULL, uam.y, 1), uae = __shfl_down_sync(FULL, uam.x, 1);
             const float ubw = __shfl_up_sync(FULL, ubm.y, 1), ube = __shfl_down_sync(FULL, ubm.x, 1);
             if (own && rb >= y0 && rb < ny) {
-                const bool near = edge_x || rb < g.sponge_w || rb >= ny - g.sponge_w;
                 const int rowb = rb * nx;
                 const int dr = edge_dist(rb, ny);
-                const float ix = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
-                const float iy = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
-                const float dx = near ? damp_at(g, dca, dr) : 1.f;
-                const float dy = near ? damp_at(g, dcb, dr) : 1.f;
+                const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+                float dx = drow, dy = drow;
+                if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+                float ix = 0.f, iy = 0.f;
+                if (rcvm) {
+                    ix = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
+                    iy = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
+                }
                 float2 zbv;
                 zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, ix, dx);
                 zbv.y = adj_cell(pe, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, iy, dy);
@@ -481,6 +493,7 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
         uam2 = uam; uam = ua0;
         ubm2 = ubm; ubm = ub0;
         ridm = rid;
+        rcvm = rcv;
         crm = cr_next;
     }
 }
