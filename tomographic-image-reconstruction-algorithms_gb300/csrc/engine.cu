@@ -231,7 +231,7 @@ void tune_cache_append(const tomo_ctx* c, const char* path) {
 // per launch) by timing each candidate on this problem (mid-sweep steps of the
 // first pass, best of three timed passes).  TOMO_STRIP_ROWS=<n> fixes the
 // choice; TOMO_TUNE_CACHE=<file> reuses a choice recorded there for the same
-// problem shape, or records the one made here.
+// problem shape, or records the one made here; TOMO_TUNE_LOG prints each candidate's time.
 tomo_status autotune(tomo_ctx* c) {
     if (c->tuned || !c->strip) { c->tuned = true; return TOMO_OK; }
     c->tuned = true;
@@ -249,6 +249,7 @@ tomo_status autotune(tomo_ctx* c) {
     }
     const int cands[5] = {2, 4, 8, 16, 32};
     const int nt = c->geo.nt, ng = c->P, reps = 8, passes = 4;
+    const bool tlog = std::getenv("TOMO_TUNE_LOG") != nullptr;   // print every candidate's time
     // trial steps k0 .. k0+reps stay inside [1, nt-2] (records are read at step q+1)
     if (nt < 4 * reps) return TOMO_OK;   // short sweeps keep the defaults
     const int k0 = nt / 2 - reps;
@@ -270,6 +271,8 @@ tomo_status autotune(tomo_ctx* c) {
                 CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
                 if (pass > 0) ms = std::min(ms, t_ms);
             }
+            if (tlog) std::fprintf(stderr, "tomo tune: %s rows %d%s %.2f us/step\n", which ? "adjoint" : "forward", rows,
+                                   which ? (" variant " + std::to_string(which - 1)).c_str() : "", 1e3 * ms / reps);
             if (which == 0 && ms < best_f) { best_f = ms; c->rows_fwd = rows; c->fwd_pair = false; }
             if (which > 0 && ms < best_a) {
                 best_a = ms; c->rows_adj = rows; c->adj_variant = which - 1; c->adj_pair = false;
@@ -289,10 +292,11 @@ tomo_status autotune(tomo_ctx* c) {
                 CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
                 if (pass > 0) ms = std::min(ms, t_ms);
             }
+            if (tlog) std::fprintf(stderr, "tomo tune: forward pair code %d %.2f us/step\n", code, 1e3 * ms / reps);
             if (ms < best_f) { best_f = ms; c->rows_fwd2 = code; c->fwd_pair = true; }
         }
         // two steps per launch (reps/2 launches cover the same steps); codes as launch_adj2_strip
-        for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows}) {
+        for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows, 2000 + rows}) {
             if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {
@@ -306,6 +310,7 @@ tomo_status autotune(tomo_ctx* c) {
                 CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
                 if (pass > 0) ms = std::min(ms, t_ms);
             }
+            if (tlog) std::fprintf(stderr, "tomo tune: adjoint pair code %d %.2f us/step\n", code, 1e3 * ms / reps);
             if (ms < best_a) { best_a = ms; c->rows_adj2 = code; c->adj_pair = true; }
         }
     }

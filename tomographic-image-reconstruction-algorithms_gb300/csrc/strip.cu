@@ -528,6 +528,135 @@ void adj2_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStrea
 }
 
 // ---------------------------------------------------------------------------
+// Two adjoint steps per launch with four cells per lane (float4): 128-cell strips overlapping
+// by one lane (4 cells) on each side, lanes 1..30 (120 cells) write.  Rows, rolling state,
+// halo argument and arithmetic are those of k_adj2_strip, so the results are identical.
+__device__ __forceinline__ float c4(const float4& v, int t) { return t == 0 ? v.x : t == 1 ? v.y : t == 2 ? v.z : v.w; }
+__device__ __forceinline__ int c4(const int4& v, int t) { return t == 0 ? v.x : t == 1 ? v.y : t == 2 ? v.z : v.w; }
+
+template <int R>
+__global__ void __launch_bounds__(WARPS * 32, 4) k_adj2q_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 120 - 4;
+    const int i = x0 + 4 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    const bool in = i >= 0 && i < nx;
+    const bool own = in && lane >= 1 && lane <= 30;
+    const float* z1 = s.z1 + gl * s.zstride;
+    const float* z2 = s.z2 + gl * s.zstride;
+    float* za = s.za + gl * s.zstride;
+    float* zb = s.zb + gl * s.zstride;
+    const float* ua = s.ua + gl * s.ustride;
+    const float* ub = s.ub + gl * s.ustride;
+    const float* rra = s.rra + gl * s.rrstride;
+    const float* rrb = s.rrb + gl * s.rrstride;
+    float* corr = s.corr + gl * s.cstride;
+    const bool edge_x = x0 < g.sponge_w || x0 + 128 > nx - g.sponge_w;
+    auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
+    const RcvMask rk = rcv_mask(g, x0, x0 + 128);
+    int dc[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) dc[t] = edge_dist(i + t, nx);
+    // rolling state at the top of iteration r, as in k_adj2_strip
+    float4 z1m = ld4(z1, (y0 - 2) * nx + i, row_ok(y0 - 2));
+    float4 z10 = ld4(z1, (y0 - 1) * nx + i, row_ok(y0 - 1));
+    float4 pzm = mul4(ld4(coef, (y0 - 2) * nx + i, row_ok(y0 - 2)), z1m);
+    float4 c0 = ld4(coef, (y0 - 1) * nx + i, row_ok(y0 - 1));
+    float4 pz0 = mul4(c0, z10);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 zam = zero, pam2 = zero, pam = zero, uam2 = zero, uam = zero, ubm2 = zero, ubm = zero;
+    int4 ridm = make_int4(-1, -1, -1, -1);
+    bool rcvm = false;
+#pragma unroll 1
+    for (int r = y0 - 1; r <= y0 + R; ++r) {
+        if (r > ny) break;
+        const int row = r * nx;
+        const bool ok = row_ok(r), okn = row_ok(r + 1);
+        const float4 z1p = ld4(z1, row + nx + i, okn);
+        const float4 cp = ld4(coef, row + nx + i, okn);
+        const float4 zz = ld4(z2, row + i, ok);
+        const float4 ua0 = ld4(ua, row + i, ok);
+        const float4 ub0 = ld4(ub, row + i, ok);
+        const bool rcv = rcv_row(g, rk, r);
+        int4 rid = make_int4(-1, -1, -1, -1);
+        if (rcv && ok) rid = *reinterpret_cast<const int4*>(g.rid + row + i);
+        const float4 pzp = mul4(cp, z1p);
+        // ---- first step: z(kz) at row r (all lanes; zero outside the grid; the halo cells
+        // x0 .. x0+2 and x0+125 .. x0+127 are not read by any owned cell's second step)
+        float4 za0 = zero;
+        {
+            const float pw = __shfl_up_sync(FULL, pz0.w, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
+            if (ok) {
+                const int dr = edge_dist(r, ny);
+                const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+                float v[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float d = edge_x ? damp_at(g, dc[t], dr) : drow;
+                    const int id = c4(rid, t);
+                    const float inj = (rcv && id >= 0) ? rra[id] : 0.f;
+                    const float e = t < 3 ? c4(pz0, t + 1) : pe;
+                    const float w = t > 0 ? c4(pz0, t - 1) : pw;
+                    v[t] = adj_cell(e, w, c4(pzm, t), c4(pzp, t), c4(pz0, t), c4(z10, t), c4(zz, t), inj, d);
+                }
+                za0 = make_float4(v[0], v[1], v[2], v[3]);
+            }
+        }
+        const float4 pa0 = mul4(c0, za0);
+        // ---- second step: z(kz-1) at row r-1, correlation of both steps at row r-1
+        const int rb = r - 1;
+        {
+            const float pw = __shfl_up_sync(FULL, pam.w, 1), pe = __shfl_down_sync(FULL, pam.x, 1);
+            const float uaw = __shfl_up_sync(FULL, uam.w, 1), uae = __shfl_down_sync(FULL, uam.x, 1);
+            const float ubw = __shfl_up_sync(FULL, ubm.w, 1), ube = __shfl_down_sync(FULL, ubm.x, 1);
+            if (own && rb >= y0 && rb < ny) {
+                const int rowb = rb * nx;
+                const int dr = edge_dist(rb, ny);
+                const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+                float4 cr = *reinterpret_cast<const float4*>(corr + rowb + i);
+                float zv[4], cv[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float d = edge_x ? damp_at(g, dc[t], dr) : drow;
+                    const int id = c4(ridm, t);
+                    const float inj = (rcvm && id >= 0) ? rrb[id] : 0.f;
+                    const float e = t < 3 ? c4(pam, t + 1) : pe;
+                    const float w = t > 0 ? c4(pam, t - 1) : pw;
+                    zv[t] = adj_cell(e, w, c4(pam2, t), c4(pa0, t), c4(pam, t), c4(zam, t), c4(z1m, t), inj, d);
+                    const float la = lap5(t < 3 ? c4(uam, t + 1) : uae, t > 0 ? c4(uam, t - 1) : uaw, c4(uam2, t),
+                                          c4(ua0, t), c4(uam, t));
+                    const float lb = lap5(t < 3 ? c4(ubm, t + 1) : ube, t > 0 ? c4(ubm, t - 1) : ubw, c4(ubm2, t),
+                                          c4(ub0, t), c4(ubm, t));
+                    cv[t] = __fmaf_rn(zv[t], lb, __fmaf_rn(c4(zam, t), la, c4(cr, t)));
+                }
+                *reinterpret_cast<float4*>(corr + rowb + i) = make_float4(cv[0], cv[1], cv[2], cv[3]);
+                *reinterpret_cast<float4*>(za + rowb + i) = zam;
+                *reinterpret_cast<float4*>(zb + rowb + i) = make_float4(zv[0], zv[1], zv[2], zv[3]);
+            }
+        }
+        z1m = z10; z10 = z1p;
+        pzm = pz0; pz0 = pzp;
+        c0 = cp;
+        zam = za0;
+        pam2 = pam; pam = pa0;
+        uam2 = uam; uam = ua0;
+        ubm2 = ubm; ubm = ub0;
+        ridm = rid;
+        rcvm = rcv;
+    }
+}
+
+template <int R>
+void adj2q_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    dim3 grid((g.nx + 119) / 120, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
+    k_adj2q_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+}
+
+// ---------------------------------------------------------------------------
 // Two forward steps per launch.  Same strip geometry as k_adj2_strip (2 cells
 // per lane, 64-cell strips overlapping by one lane each side, lanes 1..30
 // write).  u(k+1) rows y0-1 .. y0+R roll through registers and u(k+2) follows
@@ -804,13 +933,17 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     s.rra = a.rr; s.rrb = b.rr; s.rrstride = a.rrstride;
     s.corr = a.corr; s.cstride = a.cstride; s.ng = a.ng;
     cudaStream_t st = (cudaStream_t)stream;
-    // code = rows + 100 * AHEAD + 1000 * SPLIT (see k_adj2_strip)
+    // code = rows + 100 * AHEAD + 1000 * SPLIT (see k_adj2_strip); 2000 + rows: k_adj2q_strip
 #define ADJ2_CASE(R, A, S) \
     case (R) + 100 * (A) + 1000 * (S): adj2_strip<R, A, S>(g, coef, s, st); return;
 #define ADJ2_ROWS(A, S) ADJ2_CASE(4, A, S) ADJ2_CASE(8, A, S) ADJ2_CASE(16, A, S) ADJ2_CASE(32, A, S)
     switch (rows) {
         ADJ2_ROWS(0, false) ADJ2_ROWS(1, false) ADJ2_ROWS(2, false)
         ADJ2_ROWS(0, true) ADJ2_ROWS(1, true) ADJ2_ROWS(2, true)
+    case 2004: adj2q_strip<4>(g, coef, s, st); return;     // 2000 + rows: four cells per lane
+    case 2008: adj2q_strip<8>(g, coef, s, st); return;
+    case 2016: adj2q_strip<16>(g, coef, s, st); return;
+    case 2032: adj2q_strip<32>(g, coef, s, st); return;
     default: adj2_strip<8, 0, false>(g, coef, s, st); return;
     }
 #undef ADJ2_ROWS
