@@ -111,11 +111,7 @@ def run_batch(args, local, rank, world, dist):
     with ClockSampler(local) as clk:
         eps, secs = tomo.iterate_batch(ctxs, tomo.SIRT_NORM, sched, args.warmup, args.steps, ptrs, tptrs)
     clocks = clk.summary()
-    t_max = secs
-    if dist:
-        t = torch.tensor([secs], dtype=torch.float64, device=dev if dist.get_backend() == "nccl" else "cpu")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(secs, dist, dev)
     value = world * bytes_it * args.steps / t_max / 1e9
     # end to end: every step copies each phantom's records and field in from pinned host memory and
     # the field back out
@@ -331,6 +327,17 @@ def time_to_image(ctx, w, sched, d_f, d_ft, torch, dev, plain_iters=30):
             "speedup": t_plain / t_learned if reached else None}
 
 
+def max_over_ranks(x, dist, dev=None):
+    """The largest x over all ranks (x itself without a process group)."""
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=dev if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def read_tuning(path):
     """The strip-kernel choice of the autotuner, from its cache file (last line)."""
     try:
@@ -440,11 +447,7 @@ def main():
     barrier()
     ms = e0.elapsed_time(e1)
     clocks = clk.summary()
-    t_max = ms
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev if dist.get_backend() == "nccl" else "cpu")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(ms, dist, dev)
     bytes_step = algorithmic_bytes(cfg, G)
     value = world * bytes_step * args.steps / (t_max * 1e-3) / 1e9
 
@@ -459,11 +462,7 @@ def main():
         ctx.iterate(w["method"], sched, s, fa, rec_host.numpy(), ft_host.numpy())
     e2e_s = time.perf_counter() - t0
     barrier()
-    e2e_max = e2e_s
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev if dist.get_backend() == "nccl" else "cpu")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_max = float(t.item())
+    e2e_max = max_over_ranks(e2e_s, dist, dev)
     e2e_val = world * bytes_step * args.steps / e2e_max / 1e9
     h2d = 4 * (fo.size * 2 + rec.size)
     d2h = 4 * fo.size + 8

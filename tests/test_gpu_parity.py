@@ -237,10 +237,11 @@ def test_errors_are_status_codes():
         assert e.value.status == tomo.ERR_ARG
 
 
-@pytest.mark.parametrize("adj_rows", ["1004", "1108", "1216", "232", "2008", "2032"])
+@pytest.mark.parametrize("adj_rows", ["1004", "1108", "1216", "232", "2008", "2032", "4008", "4132"])
 def test_two_step_adjoint_variants_match_one_step(adj_rows, monkeypatch):
     """The two-step adjoint's variants (interior fast path, inputs read ahead, four cells per
-    lane) give the one-step kernel's bits on a grid wide enough to have interior strips (nx 256)."""
+    lane, packed FP32x2 arithmetic) give the one-step kernel's bits on a grid wide enough to
+    have interior strips (nx 256)."""
     cfg0 = small_cfg(nx=256, ny=96, nt=161, n_transducers=32, radius=40.0, ckpt_interval=12)
     fo = blob_phantom(96, 256, seed=18)
     meas = O.forward(cfg0, fo.astype(np.float64))

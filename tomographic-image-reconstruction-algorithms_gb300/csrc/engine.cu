@@ -296,7 +296,8 @@ tomo_status autotune(tomo_ctx* c) {
             if (ms < best_f) { best_f = ms; c->rows_fwd2 = code; c->fwd_pair = true; }
         }
         // two steps per launch (reps/2 launches cover the same steps); codes as launch_adj2_strip
-        for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows, 2000 + rows}) {
+        for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows, 2000 + rows,
+                         4000 + rows, 4100 + rows}) {
             if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {

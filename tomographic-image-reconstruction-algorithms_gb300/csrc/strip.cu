@@ -42,6 +42,37 @@ __device__ __forceinline__ float sponge(const DevGeo& g, int i, int j) {
 // the compiler would otherwise contract into fused multiply-adds.
 __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
 
+// Packed FP32x2 arithmetic (add/sub/mul/fma .rn.f32x2, sm_100 and later): one instruction for
+// a lane's two cells, each half rounded exactly as the scalar __fadd_rn / __fsub_rn /
+// __fmul_rn / __fmaf_rn, so results match the one-cell helpers bit for bit.
+__device__ __forceinline__ float2 pk_add(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 pk_sub(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 pk_mul(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return make_float2(mul(a.x, b.x), mul(a.y, b.y)); }
 __device__ __forceinline__ float4 mul4(float4 a, float4 b) {
     return make_float4(mul(a.x, b.x), mul(a.y, b.y), mul(a.z, b.z), mul(a.w, b.w));
@@ -58,6 +89,16 @@ __device__ __forceinline__ float adj_cell(float ce, float cw, float cs, float cn
 // ((e + w) + s) + n - 4 u
 __device__ __forceinline__ float lap5(float e, float w, float s, float n, float u) {
     return __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(e, w), s), n), mul(4.f, u));
+}
+
+// adj_cell and lap5 for a lane's two cells in packed FP32x2 (same operation order)
+__device__ __forceinline__ float2 adj_cell2(float2 ce, float2 cw, float2 cs, float2 cn, float2 cz, float2 z, float2 z2,
+                                            float2 inj, float2 d) {
+    const float2 lz = pk_sub(pk_add(pk_add(pk_add(ce, cw), cs), cn), pk_mul(make_float2(4.f, 4.f), cz));
+    return pk_mul(d, pk_add(pk_add(pk_sub(pk_mul(make_float2(2.f, 2.f), z), z2), lz), inj));
+}
+__device__ __forceinline__ float2 lap5_2(float2 e, float2 w, float2 s, float2 n, float2 u) {
+    return pk_sub(pk_add(pk_add(pk_add(e, w), s), n), pk_mul(make_float2(4.f, 4.f), u));
 }
 
 // Forward cell update d * ((2 u - up) + c * lap) + a, explicit rounding (shared by
@@ -340,7 +381,7 @@ __device__ __forceinline__ float2 ld2(const float* __restrict__ p, int64_t off, 
 
 // Rows y0 .. y0+R-1 of one warp strip.  EDGE = false: the strip, its one-cell halo and rows
 // y0-2 .. y0+R+2 lie inside the grid, so no access needs a bounds predicate.
-template <int R, int AHEAD, bool EDGE>
+template <int R, int AHEAD, bool EDGE, bool PACK>
 __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restrict__ coef, const Adj2Step& s,
                                           int x0, int y0) {
     constexpr bool PF = AHEAD >= 1;
@@ -428,7 +469,7 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
         // correlation of row r, read now for the second step of the next iteration
         float2 cr_next = make_float2(0.f, 0.f);
         if (PF && own && r >= y0 && r < yend) cr_next = *reinterpret_cast<const float2*>(corr + row + i);
-        const float2 pzp = mul2(cp, z1p);
+        const float2 pzp = PACK ? pk_mul(cp, z1p) : mul2(cp, z1p);
         // ---- first step: z(kz) at row r (all lanes; zero outside the grid)
         float2 za0 = make_float2(0.f, 0.f);
         {
@@ -445,11 +486,16 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
                     ix = rid.x >= 0 ? rra[rid.x] : 0.f;
                     iy = rid.y >= 0 ? rra[rid.y] : 0.f;
                 }
-                za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, ix, dx);
-                za0.y = adj_cell(pe, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, iy, dy);
+                if constexpr (PACK) {
+                    za0 = adj_cell2(make_float2(pz0.y, pe), make_float2(pw, pz0.x), pzm, pzp, pz0, z10, zz,
+                                    make_float2(ix, iy), make_float2(dx, dy));
+                } else {
+                    za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, ix, dx);
+                    za0.y = adj_cell(pe, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, iy, dy);
+                }
             }
         }
-        const float2 pa0 = mul2(c0, za0);
+        const float2 pa0 = PACK ? pk_mul(c0, za0) : mul2(c0, za0);
         // ---- second step: z(kz-1) at row r-1, correlation of both steps at row r-1
         const int rb = r - 1;
         {
@@ -468,18 +514,27 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
                     ix = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
                     iy = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
                 }
-                float2 zbv;
-                zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, ix, dx);
-                zbv.y = adj_cell(pe, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, iy, dy);
-                const float lax = lap5(uam.y, uaw, uam2.x, ua0.x, uam.x);
-                const float lay = lap5(uae, uam.x, uam2.y, ua0.y, uam.y);
-                const float lbx = lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x);
-                const float lby = lap5(ube, ubm.x, ubm2.y, ub0.y, ubm.y);
                 float2 cr = PF ? crm : *reinterpret_cast<const float2*>(corr + rowb + i);
-                cr.x = __fmaf_rn(zam.x, lax, cr.x);
-                cr.y = __fmaf_rn(zam.y, lay, cr.y);
-                cr.x = __fmaf_rn(zbv.x, lbx, cr.x);
-                cr.y = __fmaf_rn(zbv.y, lby, cr.y);
+                float2 zbv;
+                if constexpr (PACK) {
+                    zbv = adj_cell2(make_float2(pam.y, pe), make_float2(pw, pam.x), pam2, pa0, pam, zam, z1m,
+                                    make_float2(ix, iy), make_float2(dx, dy));
+                    const float2 la = lap5_2(make_float2(uam.y, uae), make_float2(uaw, uam.x), uam2, ua0, uam);
+                    const float2 lb = lap5_2(make_float2(ubm.y, ube), make_float2(ubw, ubm.x), ubm2, ub0, ubm);
+                    cr = pk_fma(zam, la, cr);
+                    cr = pk_fma(zbv, lb, cr);
+                } else {
+                    zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, ix, dx);
+                    zbv.y = adj_cell(pe, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, iy, dy);
+                    const float lax = lap5(uam.y, uaw, uam2.x, ua0.x, uam.x);
+                    const float lay = lap5(uae, uam.x, uam2.y, ua0.y, uam.y);
+                    const float lbx = lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x);
+                    const float lby = lap5(ube, ubm.x, ubm2.y, ub0.y, ubm.y);
+                    cr.x = __fmaf_rn(zam.x, lax, cr.x);
+                    cr.y = __fmaf_rn(zam.y, lay, cr.y);
+                    cr.x = __fmaf_rn(zbv.x, lbx, cr.x);
+                    cr.y = __fmaf_rn(zbv.y, lby, cr.y);
+                }
                 *reinterpret_cast<float2*>(corr + rowb + i) = cr;
                 *reinterpret_cast<float2*>(za + rowb + i) = zam;
                 *reinterpret_cast<float2*>(zb + rowb + i) = zbv;
@@ -502,29 +557,31 @@ __device__ __forceinline__ void adj2_rows(const DevGeo& g, const float* __restri
 // correlation row one iteration ahead; 2 reads every input one iteration ahead (more loads in
 // flight per warp).  SPLIT: warps whose strip lies inside the grid take a path without bounds
 // predicates (the compiler then overlaps more loads, at more registers).  Minimum resident
-// blocks per SM: 8 / 7 / 5 (AHEAD 0 / 1 / 2), 6 / 5 / 4 with SPLIT.
-constexpr int adj2_min_blocks(int ahead, bool split) {
-    return split ? (ahead == 2 ? 4 : 6 - ahead) : (ahead == 2 ? 5 : 8 - ahead);
+// blocks per SM: 8 / 7 / 5 (AHEAD 0 / 1 / 2), 6 / 5 / 4 with SPLIT, one fewer with PACK.
+constexpr int adj2_min_blocks(int ahead, bool split, bool pack) {
+    return (split ? (ahead == 2 ? 4 : 6 - ahead) : (ahead == 2 ? 5 : 8 - ahead)) - (pack ? 1 : 0);
 }
 
-template <int R, int AHEAD, bool SPLIT>
-__global__ void __launch_bounds__(WARPS * 32, adj2_min_blocks(AHEAD, SPLIT))
+// PACK: the cell arithmetic in packed FP32x2 instructions (same bits, fewer instructions, register
+// pairs).
+template <int R, int AHEAD, bool SPLIT, bool PACK = false>
+__global__ void __launch_bounds__(WARPS * 32, adj2_min_blocks(AHEAD, SPLIT, PACK))
     k_adj2_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
     const int warp = threadIdx.x >> 5;
     const int x0 = blockIdx.x * 60 - 2;
     const int y0 = (blockIdx.y * WARPS + warp) * R;
     if (y0 >= g.ny) return;
     if (SPLIT && x0 > 0 && x0 + 64 < g.nx && y0 >= 2 && y0 + R + 2 < g.ny)
-        adj2_rows<R, AHEAD, false>(g, coef, s, x0, y0);
+        adj2_rows<R, AHEAD, false, PACK>(g, coef, s, x0, y0);
     else
-        adj2_rows<R, AHEAD, true>(g, coef, s, x0, y0);
+        adj2_rows<R, AHEAD, true, PACK>(g, coef, s, x0, y0);
 }
 
-template <int R, int AHEAD, bool SPLIT>
+template <int R, int AHEAD, bool SPLIT, bool PACK = false>
 void adj2_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     dim3 grid((g.nx + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
-    k_adj2_strip<R, AHEAD, SPLIT><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+    k_adj2_strip<R, AHEAD, SPLIT, PACK><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -940,6 +997,14 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     switch (rows) {
         ADJ2_ROWS(0, false) ADJ2_ROWS(1, false) ADJ2_ROWS(2, false)
         ADJ2_ROWS(0, true) ADJ2_ROWS(1, true) ADJ2_ROWS(2, true)
+    case 4004: adj2_strip<4, 0, false, true>(g, coef, s, st); return;     // 4000 + rows + 100 AHEAD: PACK
+    case 4008: adj2_strip<8, 0, false, true>(g, coef, s, st); return;
+    case 4016: adj2_strip<16, 0, false, true>(g, coef, s, st); return;
+    case 4032: adj2_strip<32, 0, false, true>(g, coef, s, st); return;
+    case 4104: adj2_strip<4, 1, false, true>(g, coef, s, st); return;
+    case 4108: adj2_strip<8, 1, false, true>(g, coef, s, st); return;
+    case 4116: adj2_strip<16, 1, false, true>(g, coef, s, st); return;
+    case 4132: adj2_strip<32, 1, false, true>(g, coef, s, st); return;
     case 2004: adj2q_strip<4>(g, coef, s, st); return;     // 2000 + rows: four cells per lane
     case 2008: adj2q_strip<8>(g, coef, s, st); return;
     case 2016: adj2q_strip<16>(g, coef, s, st); return;
