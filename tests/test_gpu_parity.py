@@ -237,11 +237,12 @@ def test_errors_are_status_codes():
         assert e.value.status == tomo.ERR_ARG
 
 
-@pytest.mark.parametrize("adj_rows", ["1004", "1108", "1216", "232", "2008", "2032", "4008", "4132"])
+@pytest.mark.parametrize("adj_rows", ["1004", "1108", "1216", "232", "2008", "2032", "4008", "4132",
+                                      "3204", "3308", "3332", "3416"])
 def test_two_step_adjoint_variants_match_one_step(adj_rows, monkeypatch):
     """The two-step adjoint's variants (interior fast path, inputs read ahead, four cells per
-    lane, packed FP32x2 arithmetic) give the one-step kernel's bits on a grid wide enough to
-    have interior strips (nx 256)."""
+    lane, packed FP32x2 arithmetic, inputs staged in shared memory by cp.async) give the
+    one-step kernel's bits on a grid wide enough to have interior strips (nx 256)."""
     cfg0 = small_cfg(nx=256, ny=96, nt=161, n_transducers=32, radius=40.0, ckpt_interval=12)
     fo = blob_phantom(96, 256, seed=18)
     meas = O.forward(cfg0, fo.astype(np.float64))
@@ -269,7 +270,7 @@ def test_two_step_kernels_match_one_step(nt, monkeypatch):
     outs = []
     # fwd 104: four cells per lane; adj 104 / 208: correlation / all inputs read one row ahead
     for pair, fwd_rows, adj_rows in (("0", "4", "4"), ("1", "4", "4"), ("1", "104", "104"), ("1", "4", "208"),
-                                     ("1", "4", "2004")):
+                                     ("1", "4", "2004"), ("1", "4", "3304")):
         monkeypatch.setenv("TOMO_STRIP_ROWS", "4")
         monkeypatch.setenv("TOMO_FWD_PAIR", pair)
         monkeypatch.setenv("TOMO_FWD_PAIR_ROWS", fwd_rows)

@@ -128,22 +128,36 @@ __global__ void k_pack_input(const float* __restrict__ feat, __nv_bfloat16* __re
     }
 }
 
-// Layer 5 forward: out[p] = b5 + sum_{tap, ci} y4[p + off(tap)][ci] * w5[tap][ci] (FP32).
-__global__ void k_conv_out(const __nv_bfloat16* __restrict__ y4, const float* __restrict__ w5, const float* __restrict__ b5,
-                           float* __restrict__ out, int B, int H, int W) {
-    const int64_t HW = (int64_t)H * W, n = (int64_t)B * HW;
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t b = p / HW;
-        const int y = (int)((p % HW) / W), x = (int)(p % W);
-        float acc = b5[0];
-        for (int tap = 0; tap < 9; ++tap) {
-            const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-            if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-            const __nv_bfloat16* v = y4 + ((b * H + yy) * W + xx) * COUT;
-            for (int c = 0; c < COUT; ++c) acc = fmaf(__bfloat162float(v[c]), w5[tap * COUT + c], acc);
+// Layer 5 forward: out[p] = b5 + sum_{tap, ci} y4[p + off(tap)][ci] * w5[tap][ci] (FP32, taps
+// then channels in order).  One block row per image row (blockIdx.y = b*H + y), one thread per
+// pixel, 16-byte loads of 8 channels, the 288 weights in shared memory.
+__global__ void __launch_bounds__(128) k_conv_out(const __nv_bfloat16* __restrict__ y4, const float* __restrict__ w5,
+                                                  const float* __restrict__ b5, float* __restrict__ out, int B, int H,
+                                                  int W) {
+    __shared__ float ws[9 * COUT];
+    for (int j = threadIdx.x; j < 9 * COUT; j += blockDim.x) ws[j] = w5[j];
+    __syncthreads();
+    const int row = blockIdx.y, b = row / H, y = row - b * H;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    float acc = b5[0];
+    for (int tap = 0; tap < 9; ++tap) {
+        const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+        if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+        const uint4* v = reinterpret_cast<const uint4*>(y4 + ((int64_t)(b * H + yy) * W + xx) * COUT);
+#pragma unroll
+        for (int q = 0; q < COUT / 8; ++q) {
+            const uint4 u = v[q];
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float2 f = __bfloat1622float2(h[k]);
+                acc = fmaf(f.x, ws[tap * COUT + q * 8 + 2 * k], acc);
+                acc = fmaf(f.y, ws[tap * COUT + q * 8 + 2 * k + 1], acc);
+            }
         }
-        out[p] = acc;
     }
+    out[(int64_t)row * W + x] = acc;
 }
 
 // Masked MSE: loss partial per block, dout = 2 mask (out - tgt) / msum.
@@ -185,25 +199,31 @@ __global__ void k_conv_out_dgrad(const float* __restrict__ dout, const float* __
     }
 }
 
-// Layer 5 weight gradient partials: part[blk][tap*32+ci] and part[blk][288] (bias),
-// each block a grid-stride share of the pixels, fixed order.
+// Layer 5 weight gradient partials: part[blk][tap*32+ci] and part[blk][288] (bias), each
+// block a grid-stride share of the image rows, pixels in order within a row; thread j =
+// tap*32 + ci reads one channel of the shifted row (a warp reads 64 contiguous bytes).
 __global__ void __launch_bounds__(COUT * 9) k_conv_out_wgrad(const float* __restrict__ dout,
                                                            const __nv_bfloat16* __restrict__ y4, int B, int H, int W,
                                                            float* __restrict__ part) {
     const int j = threadIdx.x;   // tap*32 + ci
     const int tap = j / COUT, ci = j % COUT;
-    const int64_t HW = (int64_t)H * W, n = (int64_t)B * HW;
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const bool centre = tap == 4;               // covers every pixel: it also sums the bias gradient
+    const int xa = dx < 0 ? 1 : 0, xb = dx > 0 ? W - 1 : W;
     float acc = 0.f, accb = 0.f;
-    for (int64_t p = blockIdx.x; p < n; p += gridDim.x) {
-        const int64_t b = p / HW;
-        const int y = (int)((p % HW) / W), x = (int)(p % W);
-        const float d = dout[p];
-        const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-        if (yy >= 0 && yy < H && xx >= 0 && xx < W) acc = fmaf(d, __bfloat162float(y4[((b * H + yy) * W + xx) * COUT + ci]), acc);
-        if (j == 0) accb += d;
+    for (int row = blockIdx.x; row < B * H; row += gridDim.x) {
+        const int b = row / H, yy = row - b * H + dy;
+        if (yy < 0 || yy >= H) continue;
+        const float* d = dout + (int64_t)row * W;
+        const __nv_bfloat16* src = y4 + (int64_t)(b * H + yy) * W * COUT + ci;
+        for (int x = xa; x < xb; ++x) {
+            const float dv = d[x];
+            acc = fmaf(dv, __bfloat162float(src[(int64_t)(x + dx) * COUT]), acc);
+            if (centre) accb += dv;
+        }
     }
     part[(int64_t)blockIdx.x * (9 * COUT + 1) + j] = acc;
-    if (j == 0) part[(int64_t)blockIdx.x * (9 * COUT + 1) + 9 * COUT] = accb;
+    if (tap == 4 && ci == 0) part[(int64_t)blockIdx.x * (9 * COUT + 1) + 9 * COUT] = accb;
 }
 
 // Weight gradient of a 32-output-channel layer as a GEMM over pixels:
@@ -348,7 +368,7 @@ void conv32_dgrad(const __nv_bfloat16* dz, const __nv_bfloat16* wd, const __nv_b
 }
 
 void conv_out(const __nv_bfloat16* y4, const float* w5, const float* b5, float* out, int B, int H, int W, cudaStream_t st) {
-    k_conv_out<<<blocks_for((int64_t)B * H * W, 256), 256, 0, st>>>(y4, w5, b5, out, B, H, W);
+    k_conv_out<<<dim3((W + 127) / 128, B * H), 128, 0, st>>>(y4, w5, b5, out, B, H, W);
 }
 
 void loss(const float* out, const float* tgt, const float* msk, int64_t n, float inv_msum, float* dout, double* part,

@@ -714,6 +714,180 @@ void adj2q_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStre
 }
 
 // ---------------------------------------------------------------------------
+// Two adjoint steps per launch with the row inputs staged in shared memory: each warp keeps a
+// ring of D rows of z(kz+1) and the coefficient (row r+1), z(kz+2), u(q), u(q-1) and the
+// correlation (row r), filled by cp.async (16-byte copies, L2 only) D rows ahead of use, so
+// the loads in flight do not cost registers.  Strips start at x0 = 60 bx - 4, 16-byte
+// aligned, 64 cells wide, lanes 1..30 (60 cells) write; chunks outside the grid are
+// zero-filled.  The cell arithmetic is that of k_adj2_strip, so the results are identical.
+constexpr int ST_ARR = 6;                       // staged arrays per row
+constexpr int ST_ROW = ST_ARR * 64;             // floats per staged row
+
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem), "r"(ok ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <int R, int D>
+__global__ void __launch_bounds__(WARPS * 32, 7) k_adj2s_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
+    extern __shared__ float4 st_mem4[];
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 60 - 4;
+    const int i = x0 + 2 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    float* ring = reinterpret_cast<float*>(st_mem4) + warp * D * ST_ROW;
+    const bool in = i >= 0 && i < nx;
+    const bool own = in && lane >= 1 && lane <= 30;
+    const int yend = min(y0 + R, ny);
+    const float* z1 = s.z1 + gl * s.zstride;
+    const float* z2 = s.z2 + gl * s.zstride;
+    float* za = s.za + gl * s.zstride;
+    float* zb = s.zb + gl * s.zstride;
+    const float* ua = s.ua + gl * s.ustride;
+    const float* ub = s.ub + gl * s.ustride;
+    const float* rra = s.rra + gl * s.rrstride;
+    const float* rrb = s.rrb + gl * s.rrstride;
+    float* corr = s.corr + gl * s.cstride;
+    const bool edge_x = x0 < g.sponge_w || x0 + 64 > nx - g.sponge_w;
+    auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
+    const RcvMask rk = rcv_mask(g, x0, x0 + 64);
+    const int dca = edge_dist(i, nx), dcb = edge_dist(i + 1, nx);
+    // copy duty of this lane: chunk (lane & 15) of arrays 2*slot + (lane >> 4), slot 0..2
+    const int ch = lane & 15, half = lane >> 4;
+    const int cx = x0 + 4 * ch;                          // first cell of the chunk
+    const bool cx_ok = cx >= 0 && cx + 3 < nx;           // nx % 4 == 0: chunks are all in or all out
+    auto stage = [&](int t) {                           // row t of the schedule into slot t mod D
+        float* dst = ring + ((t % D + D) % D) * ST_ROW;
+        const bool r1 = cx_ok && t + 1 >= 0 && t + 1 < ny, r0 = cx_ok && t >= 0 && t < ny;
+        const int o1 = r1 ? (t + 1) * nx + cx : 0, o0 = r0 ? t * nx + cx : 0;
+        // arrays: 0 z1(t+1), 1 coef(t+1), 2 z2(t), 3 ua(t), 4 ub(t), 5 corr(t)
+        if (half == 0) {
+            cp_async16(dst + 0 * 64 + 4 * ch, z1 + o1, r1);
+            cp_async16(dst + 2 * 64 + 4 * ch, z2 + o0, r0);
+            cp_async16(dst + 4 * 64 + 4 * ch, ub + o0, r0);
+        } else {
+            cp_async16(dst + 1 * 64 + 4 * ch, coef + o1, r1);
+            cp_async16(dst + 3 * 64 + 4 * ch, ua + o0, r0);
+            cp_async16(dst + 5 * 64 + 4 * ch, corr + o0, r0);
+        }
+    };
+    float2 z1m = ld2(z1, (y0 - 2) * nx + i, row_ok(y0 - 2));
+    float2 z10 = ld2(z1, (y0 - 1) * nx + i, row_ok(y0 - 1));
+    float2 pzm = mul2(ld2(coef, (y0 - 2) * nx + i, row_ok(y0 - 2)), z1m);
+    float2 c0 = ld2(coef, (y0 - 1) * nx + i, row_ok(y0 - 1));
+    float2 pz0 = mul2(c0, z10);
+    float2 zam = make_float2(0.f, 0.f), pam2 = make_float2(0.f, 0.f), pam = make_float2(0.f, 0.f);
+    float2 uam2 = make_float2(0.f, 0.f), uam = make_float2(0.f, 0.f);
+    float2 ubm2 = make_float2(0.f, 0.f), ubm = make_float2(0.f, 0.f);
+    float2 crm = make_float2(0.f, 0.f);
+    int2 ridm = make_int2(-1, -1);
+    bool rcvm = false;
+    const int rlast = min(y0 + R, ny);                   // the loop covers rows y0-1 .. rlast
+#pragma unroll
+    for (int t = 0; t < D; ++t) {                        // prologue: rows y0-1 .. y0+D-2
+        if (y0 - 1 + t <= rlast) stage(y0 - 1 + t);
+        cp_async_commit();
+    }
+#pragma unroll 1
+    for (int r = y0 - 1; r <= rlast; ++r) {
+        const int row = r * nx;
+        const bool ok = row_ok(r);
+        cp_async_wait<D - 1>();                          // this lane's copies of row r are done
+        __syncwarp();                                    // ... and every lane's
+        const float* sr = ring + ((r % D + D) % D) * ST_ROW + 2 * lane;
+        const float2 z1p = *reinterpret_cast<const float2*>(sr + 0 * 64);
+        const float2 cp = *reinterpret_cast<const float2*>(sr + 1 * 64);
+        const float2 zz = *reinterpret_cast<const float2*>(sr + 2 * 64);
+        const float2 ua0 = *reinterpret_cast<const float2*>(sr + 3 * 64);
+        const float2 ub0 = *reinterpret_cast<const float2*>(sr + 4 * 64);
+        const float2 cr_next = *reinterpret_cast<const float2*>(sr + 5 * 64);
+        __syncwarp();                                    // the slot is free for row r+D
+        if (r + D <= rlast) stage(r + D);
+        cp_async_commit();
+        const bool rcv = rcv_row(g, rk, r);
+        int2 rid = make_int2(-1, -1);
+        if (rcv && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
+        const float2 pzp = mul2(cp, z1p);
+        float2 za0 = make_float2(0.f, 0.f);
+        {
+            const float pw = __shfl_up_sync(FULL, pz0.y, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
+            if (ok) {
+                const int dr = edge_dist(r, ny);
+                const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+                float dx = drow, dy = drow;
+                if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+                float ix = 0.f, iy = 0.f;
+                if (rcv) {
+                    ix = rid.x >= 0 ? rra[rid.x] : 0.f;
+                    iy = rid.y >= 0 ? rra[rid.y] : 0.f;
+                }
+                za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, ix, dx);
+                za0.y = adj_cell(pe, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, iy, dy);
+            }
+        }
+        const float2 pa0 = mul2(c0, za0);
+        const int rb = r - 1;
+        {
+            const float pw = __shfl_up_sync(FULL, pam.y, 1), pe = __shfl_down_sync(FULL, pam.x, 1);
+            const float uaw = __shfl_up_sync(FULL, uam.y, 1), uae = __shfl_down_sync(FULL, uam.x, 1);
+            const float ubw = __shfl_up_sync(FULL, ubm.y, 1), ube = __shfl_down_sync(FULL, ubm.x, 1);
+            if (own && rb >= y0 && rb < ny) {
+                const int rowb = rb * nx;
+                const int dr = edge_dist(rb, ny);
+                const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+                float dx = drow, dy = drow;
+                if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+                float ix = 0.f, iy = 0.f;
+                if (rcvm) {
+                    ix = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
+                    iy = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
+                }
+                float2 zbv;
+                zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, ix, dx);
+                zbv.y = adj_cell(pe, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, iy, dy);
+                const float lax = lap5(uam.y, uaw, uam2.x, ua0.x, uam.x);
+                const float lay = lap5(uae, uam.x, uam2.y, ua0.y, uam.y);
+                const float lbx = lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x);
+                const float lby = lap5(ube, ubm.x, ubm2.y, ub0.y, ubm.y);
+                float2 cr = crm;
+                cr.x = __fmaf_rn(zam.x, lax, cr.x);
+                cr.y = __fmaf_rn(zam.y, lay, cr.y);
+                cr.x = __fmaf_rn(zbv.x, lbx, cr.x);
+                cr.y = __fmaf_rn(zbv.y, lby, cr.y);
+                *reinterpret_cast<float2*>(corr + rowb + i) = cr;
+                *reinterpret_cast<float2*>(za + rowb + i) = zam;
+                *reinterpret_cast<float2*>(zb + rowb + i) = zbv;
+            }
+        }
+        z1m = z10; z10 = z1p;
+        pzm = pz0; pz0 = pzp;
+        c0 = cp;
+        zam = za0;
+        pam2 = pam; pam = pa0;
+        uam2 = uam; uam = ua0;
+        ubm2 = ubm; ubm = ub0;
+        ridm = rid;
+        rcvm = rcv;
+        crm = cr_next;
+    }
+    cp_async_wait<0>();                                  // nothing left in flight at exit
+}
+
+template <int R, int D>
+void adj2s_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    const size_t smem = sizeof(float) * WARPS * D * ST_ROW;
+    dim3 grid((g.nx + 2 + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
+    k_adj2s_strip<R, D><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
+}
+
+// ---------------------------------------------------------------------------
 // Two forward steps per launch.  Same strip geometry as k_adj2_strip (2 cells
 // per lane, 64-cell strips overlapping by one lane each side, lanes 1..30
 // write).  u(k+1) rows y0-1 .. y0+R roll through registers and u(k+2) follows
@@ -1005,6 +1179,18 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     case 4108: adj2_strip<8, 1, false, true>(g, coef, s, st); return;
     case 4116: adj2_strip<16, 1, false, true>(g, coef, s, st); return;
     case 4132: adj2_strip<32, 1, false, true>(g, coef, s, st); return;
+    case 3204: adj2s_strip<4, 2>(g, coef, s, st); return;    // 3000 + 100 D + rows: staged, D rows ahead
+    case 3208: adj2s_strip<8, 2>(g, coef, s, st); return;
+    case 3216: adj2s_strip<16, 2>(g, coef, s, st); return;
+    case 3232: adj2s_strip<32, 2>(g, coef, s, st); return;
+    case 3304: adj2s_strip<4, 3>(g, coef, s, st); return;
+    case 3308: adj2s_strip<8, 3>(g, coef, s, st); return;
+    case 3316: adj2s_strip<16, 3>(g, coef, s, st); return;
+    case 3332: adj2s_strip<32, 3>(g, coef, s, st); return;
+    case 3404: adj2s_strip<4, 4>(g, coef, s, st); return;
+    case 3408: adj2s_strip<8, 4>(g, coef, s, st); return;
+    case 3416: adj2s_strip<16, 4>(g, coef, s, st); return;
+    case 3432: adj2s_strip<32, 4>(g, coef, s, st); return;
     case 2004: adj2q_strip<4>(g, coef, s, st); return;     // 2000 + rows: four cells per lane
     case 2008: adj2q_strip<8>(g, coef, s, st); return;
     case 2016: adj2q_strip<16>(g, coef, s, st); return;

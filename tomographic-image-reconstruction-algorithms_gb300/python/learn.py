@@ -202,7 +202,7 @@ def train(net, feats, tgts, mask, epochs, batch=16, lr=1e-3, seed=0, log=print):
             cur = lr * 0.5 * (1 + np.cos(np.pi * s / steps))      # cosine decay
             acc += net.train_step_device(fb.data_ptr(), tb.data_ptr(), bm.data_ptr(), batch, H, W, cur)
             s += 1
-        losses.append(acc / (M // batch))
+        losses.append(acc / max(M // batch, 1))
         log(f"  epoch {ep}: loss {losses[-1]:.3e}, {time.time() - t0:.1f} s")
     return losses, time.time() - t0
 
@@ -284,6 +284,8 @@ def main():
         report["pairs"] = int(feats.shape[0])
         report["data_seconds"] = t_data
         nval = max(16, int(0.05 * feats.shape[0]) // 16 * 16)      # held out: the last phantoms
+        if feats.shape[0] < nval + 16:
+            raise SystemExit(f"{feats.shape[0]} pairs: need at least {nval + 16} (more phantoms or iterations)")
         fv, tv = feats[-nval:], tgts[-nval:]
         feats, tgts = feats[:-nval], tgts[:-nval]
         report["baseline_loss"] = baselines(fv, tv, m, args.lookahead)
