@@ -297,7 +297,9 @@ tomo_status autotune(tomo_ctx* c) {
         }
         // two steps per launch (reps/2 launches cover the same steps); codes as launch_adj2_strip
         for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows, 2000 + rows,
-                         4000 + rows, 4100 + rows, 3200 + rows, 3300 + rows, 3400 + rows}) {
+                         4000 + rows, 4100 + rows, 3200 + rows, 3300 + rows, 3400 + rows, 5200 + rows,
+                         5300 + rows}) {
+            if (code >= 5000 && rows < 16) continue;        // the 8-block staged build exists for rows 16, 32
             if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {

@@ -731,8 +731,10 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-template <int R, int D>
-__global__ void __launch_bounds__(WARPS * 32, 7) k_adj2s_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
+// MB: minimum resident blocks per SM for the register allocator (7: 72 registers; 8: 64, one
+// wave of C2's 1152 blocks, at the price of a few spilled values).
+template <int R, int D, int MB = 7>
+__global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
     extern __shared__ float4 st_mem4[];
     const int nx = g.nx, ny = g.ny;
     const int gl = blockIdx.z;
@@ -762,20 +764,19 @@ __global__ void __launch_bounds__(WARPS * 32, 7) k_adj2s_strip(DevGeo g, const f
     const int ch = lane & 15, half = lane >> 4;
     const int cx = x0 + 4 * ch;                          // first cell of the chunk
     const bool cx_ok = cx >= 0 && cx + 3 < nx;           // nx % 4 == 0: chunks are all in or all out
+    // staged arrays: 0 z1(t+1), 1 coef(t+1), 2 z2(t), 3 ua(t), 4 ub(t), 5 corr(t); lanes 0-15
+    // copy arrays 0, 2, 4 and lanes 16-31 arrays 1, 3, 5, so each lane holds three sources
+    const float* srcA = half ? coef : z1;               // row t+1
+    const float* srcB = half ? ua : z2;                 // row t
+    const float* srcC = half ? corr : ub;               // row t
+    const int dofs = half * 64 + 4 * ch;
     auto stage = [&](int t) {                           // row t of the schedule into slot t mod D
-        float* dst = ring + ((t % D + D) % D) * ST_ROW;
+        float* dst = ring + ((t % D + D) % D) * ST_ROW + dofs;
         const bool r1 = cx_ok && t + 1 >= 0 && t + 1 < ny, r0 = cx_ok && t >= 0 && t < ny;
         const int o1 = r1 ? (t + 1) * nx + cx : 0, o0 = r0 ? t * nx + cx : 0;
-        // arrays: 0 z1(t+1), 1 coef(t+1), 2 z2(t), 3 ua(t), 4 ub(t), 5 corr(t)
-        if (half == 0) {
-            cp_async16(dst + 0 * 64 + 4 * ch, z1 + o1, r1);
-            cp_async16(dst + 2 * 64 + 4 * ch, z2 + o0, r0);
-            cp_async16(dst + 4 * 64 + 4 * ch, ub + o0, r0);
-        } else {
-            cp_async16(dst + 1 * 64 + 4 * ch, coef + o1, r1);
-            cp_async16(dst + 3 * 64 + 4 * ch, ua + o0, r0);
-            cp_async16(dst + 5 * 64 + 4 * ch, corr + o0, r0);
-        }
+        cp_async16(dst + 0 * 64, srcA + o1, r1);
+        cp_async16(dst + 2 * 64, srcB + o0, r0);
+        cp_async16(dst + 4 * 64, srcC + o0, r0);
     };
     float2 z1m = ld2(z1, (y0 - 2) * nx + i, row_ok(y0 - 2));
     float2 z10 = ld2(z1, (y0 - 1) * nx + i, row_ok(y0 - 1));
@@ -879,12 +880,12 @@ __global__ void __launch_bounds__(WARPS * 32, 7) k_adj2s_strip(DevGeo g, const f
     cp_async_wait<0>();                                  // nothing left in flight at exit
 }
 
-template <int R, int D>
+template <int R, int D, int MB = 7>
 void adj2s_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     const size_t smem = sizeof(float) * WARPS * D * ST_ROW;
     dim3 grid((g.nx + 2 + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
-    k_adj2s_strip<R, D><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
+    k_adj2s_strip<R, D, MB><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1191,6 +1192,10 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     case 3408: adj2s_strip<8, 4>(g, coef, s, st); return;
     case 3416: adj2s_strip<16, 4>(g, coef, s, st); return;
     case 3432: adj2s_strip<32, 4>(g, coef, s, st); return;
+    case 5216: adj2s_strip<16, 2, 8>(g, coef, s, st); return;   // 5000 + 100 D + rows: staged, 8 blocks
+    case 5232: adj2s_strip<32, 2, 8>(g, coef, s, st); return;
+    case 5316: adj2s_strip<16, 3, 8>(g, coef, s, st); return;
+    case 5332: adj2s_strip<32, 3, 8>(g, coef, s, st); return;
     case 2004: adj2q_strip<4>(g, coef, s, st); return;     // 2000 + rows: four cells per lane
     case 2008: adj2q_strip<8>(g, coef, s, st); return;
     case 2016: adj2q_strip<16>(g, coef, s, st); return;
