@@ -723,9 +723,8 @@ void adj2q_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStre
 constexpr int ST_ARR = 6;                       // staged arrays per row
 constexpr int ST_ROW = ST_ARR * 64;             // floats per staged row
 
-__device__ __forceinline__ void cp_async16(float* smem, const float* gmem, bool ok) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem), "r"(ok ? 16 : 0));
+__device__ __forceinline__ void cp_async16(unsigned smem_addr, const float* gmem, bool ok) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr), "l"(gmem), "r"(ok ? 16 : 0));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
@@ -769,14 +768,15 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
     const float* srcA = half ? coef : z1;               // row t+1
     const float* srcB = half ? ua : z2;                 // row t
     const float* srcC = half ? corr : ub;               // row t
-    const int dofs = half * 64 + 4 * ch;
-    auto stage = [&](int t) {                           // row t of the schedule into slot t mod D
-        float* dst = ring + ((t % D + D) % D) * ST_ROW + dofs;
+    // shared-memory byte address of this lane's copy target in slot 0
+    const unsigned ring_s = (unsigned)__cvta_generic_to_shared(ring) + 4u * (unsigned)(half * 64 + 4 * ch);
+    auto stage = [&](int t, int slot) {                 // row t of the schedule into `slot`
+        const unsigned dst = ring_s + 4u * (unsigned)(slot * ST_ROW);
         const bool r1 = cx_ok && t + 1 >= 0 && t + 1 < ny, r0 = cx_ok && t >= 0 && t < ny;
-        const int o1 = r1 ? (t + 1) * nx + cx : 0, o0 = r0 ? t * nx + cx : 0;
-        cp_async16(dst + 0 * 64, srcA + o1, r1);
-        cp_async16(dst + 2 * 64, srcB + o0, r0);
-        cp_async16(dst + 4 * 64, srcC + o0, r0);
+        const int o0 = t * nx + cx;
+        cp_async16(dst, srcA + (r1 ? o0 + nx : 0), r1);
+        cp_async16(dst + 4u * 2 * 64, srcB + (r0 ? o0 : 0), r0);
+        cp_async16(dst + 4u * 4 * 64, srcC + (r0 ? o0 : 0), r0);
     };
     float2 z1m = ld2(z1, (y0 - 2) * nx + i, row_ok(y0 - 2));
     float2 z10 = ld2(z1, (y0 - 1) * nx + i, row_ok(y0 - 1));
@@ -790,18 +790,20 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
     int2 ridm = make_int2(-1, -1);
     bool rcvm = false;
     const int rlast = min(y0 + R, ny);                   // the loop covers rows y0-1 .. rlast
+    // row y0-1 goes to slot 0, row y0-1+t to slot t mod D
 #pragma unroll
     for (int t = 0; t < D; ++t) {                        // prologue: rows y0-1 .. y0+D-2
-        if (y0 - 1 + t <= rlast) stage(y0 - 1 + t);
+        if (y0 - 1 + t <= rlast) stage(y0 - 1 + t, t);
         cp_async_commit();
     }
+    int slot = 0;                                        // slot of row r
 #pragma unroll 1
     for (int r = y0 - 1; r <= rlast; ++r) {
         const int row = r * nx;
         const bool ok = row_ok(r);
         cp_async_wait<D - 1>();                          // this lane's copies of row r are done
         __syncwarp();                                    // ... and every lane's
-        const float* sr = ring + ((r % D + D) % D) * ST_ROW + 2 * lane;
+        const float* sr = ring + slot * ST_ROW + 2 * lane;
         const float2 z1p = *reinterpret_cast<const float2*>(sr + 0 * 64);
         const float2 cp = *reinterpret_cast<const float2*>(sr + 1 * 64);
         const float2 zz = *reinterpret_cast<const float2*>(sr + 2 * 64);
@@ -809,8 +811,9 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
         const float2 ub0 = *reinterpret_cast<const float2*>(sr + 4 * 64);
         const float2 cr_next = *reinterpret_cast<const float2*>(sr + 5 * 64);
         __syncwarp();                                    // the slot is free for row r+D
-        if (r + D <= rlast) stage(r + D);
+        if (r + D <= rlast) stage(r + D, slot);
         cp_async_commit();
+        slot = slot + 1 == D ? 0 : slot + 1;
         const bool rcv = rcv_row(g, rk, r);
         int2 rid = make_int2(-1, -1);
         if (rcv && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
