@@ -260,6 +260,31 @@ def test_two_step_adjoint_variants_match_one_step(adj_rows, monkeypatch):
     assert outs[0][1] == outs[1][1]
 
 
+@pytest.mark.parametrize("fwd_rows", ["108", "3208", "3316", "3232"])
+def test_two_step_forward_variants_match_one_step(fwd_rows, monkeypatch):
+    """The two-step forward's variants (four cells per lane, inputs staged in shared memory)
+    give the one-step kernel's records and gradients bit for bit on a grid with interior
+    strips (nx 256), for an odd step count."""
+    kw = dict(nx=256, ny=96, nt=161, n_transducers=32, radius=40.0, ckpt_interval=12)
+    cfg0 = small_cfg(**kw)
+    fo = blob_phantom(96, 256, seed=28)
+    meas = O.forward(cfg0, fo.astype(np.float64))
+    f0 = blob_phantom(96, 256, seed=29, amp=0.01)
+    outs = []
+    for pair in ("0", "1"):
+        monkeypatch.setenv("TOMO_STRIP_ROWS", "4")
+        monkeypatch.setenv("TOMO_FWD_PAIR", pair)
+        monkeypatch.setenv("TOMO_FWD_PAIR_ROWS", fwd_rows)
+        monkeypatch.setenv("TOMO_ADJ_PAIR", "0")
+        with tomo.Context(small_cfg(**kw)) as ctx:
+            rec = ctx.forward(fo)
+            dfg, _, r2 = ctx.gradient(f0, meas)
+        outs.append((rec, dfg, r2))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    assert outs[0][2] == outs[1][2]
+
+
 @pytest.mark.parametrize("nt", [180, 181])
 def test_two_step_kernels_match_one_step(nt, monkeypatch):
     """Two time steps per launch (forward and adjoint) give the same bits as one."""
@@ -268,9 +293,10 @@ def test_two_step_kernels_match_one_step(nt, monkeypatch):
     meas = O.forward(cfg0, fo.astype(np.float64))
     f0 = blob_phantom(64, 72, seed=9, amp=0.01)
     outs = []
-    # fwd 104: four cells per lane; adj 104 / 208: correlation / all inputs read one row ahead
+    # fwd 104: four cells per lane; adj 104 / 208: correlation / all inputs read one row ahead;
+    # 3xxx: inputs staged in shared memory (forward and adjoint)
     for pair, fwd_rows, adj_rows in (("0", "4", "4"), ("1", "4", "4"), ("1", "104", "104"), ("1", "4", "208"),
-                                     ("1", "4", "2004"), ("1", "4", "3304")):
+                                     ("1", "4", "2004"), ("1", "3304", "3304"), ("1", "3208", "3208")):
         monkeypatch.setenv("TOMO_STRIP_ROWS", "4")
         monkeypatch.setenv("TOMO_FWD_PAIR", pair)
         monkeypatch.setenv("TOMO_FWD_PAIR_ROWS", fwd_rows)

@@ -253,7 +253,9 @@ tomo_status autotune(tomo_ctx* c) {
     // trial steps k0 .. k0+reps stay inside [1, nt-2] (records are read at step q+1)
     if (nt < 4 * reps) return TOMO_OK;   // short sweeps keep the defaults
     const int k0 = nt / 2 - reps;
-    float best_f = 1e30f, best_a = 1e30f;
+    float best_a = 1e30f;
+    float best_f1 = 1e30f, best_f2 = 1e30f;    // best one-step and two-step forward
+    int rows_f1 = c->rows_fwd, code_f2 = c->rows_fwd2;
     // forward: rows per warp; adjoint: rows per warp x register/unroll variant
     for (int rows : cands) {
         if (rows > 4 * c->geo.ny) continue;
@@ -273,12 +275,13 @@ tomo_status autotune(tomo_ctx* c) {
             }
             if (tlog) std::fprintf(stderr, "tomo tune: %s rows %d%s %.2f us/step\n", which ? "adjoint" : "forward", rows,
                                    which ? (" variant " + std::to_string(which - 1)).c_str() : "", 1e3 * ms / reps);
-            if (which == 0 && ms < best_f) { best_f = ms; c->rows_fwd = rows; c->fwd_pair = false; }
+            if (which == 0 && ms < best_f1) { best_f1 = ms; rows_f1 = rows; }
             if (which > 0 && ms < best_a) {
                 best_a = ms; c->rows_adj = rows; c->adj_variant = which - 1; c->adj_pair = false;
             }
         }
-        for (int code : {rows, 100 + rows}) {   // two forward steps per launch, 2 or 4 cells per lane
+        // two forward steps per launch: 2 or 4 cells per lane, or inputs staged in shared memory
+        for (int code : {rows, 100 + rows, 3200 + rows, 3300 + rows}) {
             if (rows < 4 || c->S < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {
@@ -293,7 +296,7 @@ tomo_status autotune(tomo_ctx* c) {
                 if (pass > 0) ms = std::min(ms, t_ms);
             }
             if (tlog) std::fprintf(stderr, "tomo tune: forward pair code %d %.2f us/step\n", code, 1e3 * ms / reps);
-            if (ms < best_f) { best_f = ms; c->rows_fwd2 = code; c->fwd_pair = true; }
+            if (ms < best_f2) { best_f2 = ms; code_f2 = code; }
         }
         // two steps per launch (reps/2 launches cover the same steps); codes as launch_adj2_strip
         for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows, 2000 + rows,
@@ -317,6 +320,11 @@ tomo_status autotune(tomo_ctx* c) {
             if (ms < best_a) { best_a = ms; c->rows_adj2 = code; c->adj_pair = true; }
         }
     }
+    // A two-step forward must win clearly: inside a sweep it also carries the odd leftover step,
+    // the sensor gather of two slices and the checkpoint copies, which the trial does not time.
+    c->rows_fwd = rows_f1;
+    c->rows_fwd2 = code_f2;
+    c->fwd_pair = best_f2 < 0.97f * best_f1;
     CU(c, cudaGetLastError());
     if (cache && *cache) tune_cache_append(c, cache);
     return TOMO_OK;

@@ -1100,6 +1100,137 @@ void fwd2q_strip(const DevGeo& g, const float* coef, const Fwd2Step& s, cudaStre
     k_fwd2q_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
 }
 
+// Two forward steps per launch with the row inputs staged in shared memory (the forward
+// counterpart of k_adj2s_strip): a per-warp ring of D rows of u(k) (row r+1), u(k-1) and the
+// coefficient (row r), filled by 16-byte cp.async copies D rows ahead.  Strips start at
+// x0 = 60 bx - 4 (16-byte aligned), lanes 1..30 write; the halo lanes' outer cells need no
+// neighbour loads (no owned cell reads their first-step values).  Same arithmetic as
+// k_fwd2_strip, so the results are identical.
+constexpr int FS_ARR = 3;
+constexpr int FS_ROW = FS_ARR * 64;
+
+template <int R, int D>
+__global__ void __launch_bounds__(WARPS * 32, 8) k_fwd2s_strip(DevGeo g, const float* __restrict__ coef, Fwd2Step s) {
+    extern __shared__ float4 fs_mem4[];
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    if (blockIdx.y == gridDim.y - 1) {
+        if (blockIdx.x != 0) return;
+        if (s.gka >= 2) gather_slice(g, s.up + gl * s.gstride, gl, s.g0, s.gka, s.gmeas, s.gout);
+        if (s.gkb >= 2) gather_slice(g, s.uc + gl * s.gstride, gl, s.g0, s.gkb, s.gmeas, s.gout);
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 60 - 4;
+    const int i = x0 + 2 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    float* ring = reinterpret_cast<float*>(fs_mem4) + warp * D * FS_ROW;
+    const bool in = i >= 0 && i < nx;
+    const bool own = in && lane >= 1 && lane <= 30;
+    const float* uc = s.uc + gl * s.gstride;
+    const float* up = s.up + gl * s.gstride;
+    float* u1 = s.u1 + gl * s.gstride;
+    float* u2 = s.u2 + gl * s.gstride;
+    float* ck1 = s.ck1 ? s.ck1 + gl * s.ckstride : nullptr;
+    float* ck2 = s.ck2 ? s.ck2 + gl * s.ckstride : nullptr;
+    const bool edge_x = x0 < g.sponge_w || x0 + 64 > nx - g.sponge_w;
+    const int32_t* em = g.emit + (int64_t)(s.g0 + gl) * g.gs;
+    const bool src1 = s.k < g.n_src_steps, src2 = s.k + 1 < g.n_src_steps;
+    const float a1 = src1 ? g.src[s.k] : 0.f, a2 = src2 ? g.src[s.k + 1] : 0.f;
+    auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
+    const int dca = edge_dist(i, nx), dcb = edge_dist(i + 1, nx);
+    // copy duty: lanes 0-15 stage u(k) (row t+1) and the coefficient (row t), lanes 16-31
+    // u(k-1) (row t); chunk (lane & 15) of each
+    const int ch = lane & 15, half = lane >> 4;
+    const int cx = x0 + 4 * ch;
+    const bool cx_ok = cx >= 0 && cx + 3 < nx;
+    const float* srcA = half ? up : uc;
+    const unsigned ring_s = (unsigned)__cvta_generic_to_shared(ring) + 4u * (unsigned)(half * 64 + 4 * ch);
+    auto stage = [&](int t, int slot) {
+        const unsigned dst = ring_s + 4u * (unsigned)(slot * FS_ROW);
+        const bool r1 = cx_ok && t + 1 >= 0 && t + 1 < ny, r0 = cx_ok && t >= 0 && t < ny;
+        const int o0 = t * nx + cx;
+        // slot layout: [0] u(k) row t+1, [1] u(k-1) row t, [2] coefficient row t
+        if (half == 0) {
+            cp_async16(dst, srcA + (r1 ? o0 + nx : 0), r1);
+            cp_async16(dst + 4u * 2 * 64, coef + (r0 ? o0 : 0), r0);
+        } else {
+            cp_async16(dst, srcA + (r0 ? o0 : 0), r0);
+        }
+    };
+    float2 u0m = ld2(uc, (y0 - 2) * nx + i, row_ok(y0 - 2));
+    float2 u00 = ld2(uc, (y0 - 1) * nx + i, row_ok(y0 - 1));
+    float2 cm = ld2(coef, (y0 - 2) * nx + i, row_ok(y0 - 2));
+    float2 v1m2 = make_float2(0.f, 0.f), v1m = make_float2(0.f, 0.f);
+    const int rlast = min(y0 + R, ny);
+#pragma unroll
+    for (int t = 0; t < D; ++t) {
+        if (y0 - 1 + t <= rlast) stage(y0 - 1 + t, t);
+        cp_async_commit();
+    }
+    int slot = 0;
+#pragma unroll 1
+    for (int r = y0 - 1; r <= rlast; ++r) {
+        const int row = r * nx;
+        const bool ok = row_ok(r);
+        cp_async_wait<D - 1>();
+        __syncwarp();
+        const float* sr = ring + slot * FS_ROW + 2 * lane;
+        const float2 u0p = *reinterpret_cast<const float2*>(sr);
+        const float2 p = *reinterpret_cast<const float2*>(sr + 64);
+        const float2 c0 = *reinterpret_cast<const float2*>(sr + 128);
+        __syncwarp();
+        if (r + D <= rlast) stage(r + D, slot);
+        cp_async_commit();
+        slot = slot + 1 == D ? 0 : slot + 1;
+        // ---- u(k+1) at row r, all lanes (zero outside the grid)
+        const float w = __shfl_up_sync(FULL, u00.y, 1), e = __shfl_down_sync(FULL, u00.x, 1);
+        float2 v10 = make_float2(0.f, 0.f);
+        if (ok) {
+            const int dr = edge_dist(r, ny);
+            const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+            float dx = drow, dy = drow;
+            if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+            const float ax = src1 ? emit_at(em, g.gs, row + i, a1) : 0.f;
+            const float ay = src1 ? emit_at(em, g.gs, row + i + 1, a1) : 0.f;
+            v10.x = fwd_cell(u00.y, w, u0m.x, u0p.x, u00.x, p.x, c0.x, dx, ax);
+            v10.y = fwd_cell(e, u00.x, u0m.y, u0p.y, u00.y, p.y, c0.y, dy, ay);
+        }
+        // ---- u(k+2) at row r-1
+        const int rb = r - 1;
+        const float w2 = __shfl_up_sync(FULL, v1m.y, 1), e2 = __shfl_down_sync(FULL, v1m.x, 1);
+        if (own && rb >= y0 && rb < ny) {
+            const int rowb = rb * nx;
+            const int dr = edge_dist(rb, ny);
+            const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+            float dx = drow, dy = drow;
+            if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+            const float ax = src2 ? emit_at(em, g.gs, rowb + i, a2) : 0.f;
+            const float ay = src2 ? emit_at(em, g.gs, rowb + i + 1, a2) : 0.f;
+            float2 v2;
+            v2.x = fwd_cell(v1m.y, w2, v1m2.x, v10.x, v1m.x, u0m.x, cm.x, dx, ax);
+            v2.y = fwd_cell(e2, v1m.x, v1m2.y, v10.y, v1m.y, u0m.y, cm.y, dy, ay);
+            *reinterpret_cast<float2*>(u1 + rowb + i) = v1m;
+            *reinterpret_cast<float2*>(u2 + rowb + i) = v2;
+            if (ck1) *reinterpret_cast<float2*>(ck1 + rowb + i) = v1m;
+            if (ck2) *reinterpret_cast<float2*>(ck2 + rowb + i) = v2;
+        }
+        u0m = u00; u00 = u0p;
+        cm = c0;
+        v1m2 = v1m; v1m = v10;
+    }
+    cp_async_wait<0>();
+}
+
+template <int R, int D>
+void fwd2s_strip(const DevGeo& g, const float* coef, const Fwd2Step& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    const size_t smem = sizeof(float) * WARPS * D * FS_ROW;
+    dim3 grid((g.nx + 2 + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block + 1, s.ng);   // + gather row
+    k_fwd2s_strip<R, D><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
+}
+
 template <int R>
 void fwd2_strip(const DevGeo& g, const float* coef, const Fwd2Step& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
@@ -1156,6 +1287,14 @@ void launch_fwd2_strip(int rows, const DevGeo& g, const float* coef, const FwdSt
     case 108: fwd2q_strip<8>(g, coef, s, st); break;
     case 116: fwd2q_strip<16>(g, coef, s, st); break;
     case 132: fwd2q_strip<32>(g, coef, s, st); break;
+    case 3204: fwd2s_strip<4, 2>(g, coef, s, st); break;     // 3000 + 100 D + rows: staged
+    case 3208: fwd2s_strip<8, 2>(g, coef, s, st); break;
+    case 3216: fwd2s_strip<16, 2>(g, coef, s, st); break;
+    case 3232: fwd2s_strip<32, 2>(g, coef, s, st); break;
+    case 3304: fwd2s_strip<4, 3>(g, coef, s, st); break;
+    case 3308: fwd2s_strip<8, 3>(g, coef, s, st); break;
+    case 3316: fwd2s_strip<16, 3>(g, coef, s, st); break;
+    case 3332: fwd2s_strip<32, 3>(g, coef, s, st); break;
     default: fwd2_strip<8>(g, coef, s, st); break;
     }
 }
