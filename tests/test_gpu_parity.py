@@ -260,6 +260,32 @@ def test_two_step_adjoint_variants_match_one_step(adj_rows, monkeypatch):
     assert outs[0][1] == outs[1][1]
 
 
+@pytest.mark.parametrize("rows", ["3204", "3308", "3316"])
+def test_staged_one_step_forward_matches(rows, monkeypatch):
+    """The one-step forward with staged inputs gives the register kernel's records and
+    gradients bit for bit (nx 256: interior strips; ny 96: with 16-row bands the last block is
+    ragged)."""
+    kw = dict(nx=256, ny=96, nt=161, n_transducers=32, radius=40.0, ckpt_interval=12)
+    cfg0 = small_cfg(**kw)
+    fo = blob_phantom(96, 256, seed=38)
+    meas = O.forward(cfg0, fo.astype(np.float64))
+    f0 = blob_phantom(96, 256, seed=39, amp=0.01)
+    outs = []
+    for r in ("4", rows):
+        monkeypatch.setenv("TOMO_STRIP_ROWS", "4")
+        monkeypatch.setenv("TOMO_FWD_ROWS", r)
+        monkeypatch.setenv("TOMO_FWD_PAIR", "0")
+        monkeypatch.setenv("TOMO_ADJ_PAIR", "0")
+        monkeypatch.setenv("TOMO_ADJ_VARIANT", "0")
+        with tomo.Context(small_cfg(**kw)) as ctx:
+            rec = ctx.forward(fo)
+            dfg, _, r2 = ctx.gradient(f0, meas)
+        outs.append((rec, dfg, r2))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    assert outs[0][2] == outs[1][2]
+
+
 @pytest.mark.parametrize("fwd_rows", ["108", "3208", "3316", "3232"])
 def test_two_step_forward_variants_match_one_step(fwd_rows, monkeypatch):
     """The two-step forward's variants (four cells per lane, inputs staged in shared memory)

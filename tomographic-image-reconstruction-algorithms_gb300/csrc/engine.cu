@@ -240,6 +240,7 @@ tomo_status autotune(tomo_ctx* c) {
     if (const char* e = std::getenv("TOMO_STRIP_ROWS")) {
         c->rows_fwd = c->rows_adj = c->rows_adj2 = std::atoi(e);
         if (const char* v = std::getenv("TOMO_ADJ_VARIANT")) c->adj_variant = std::atoi(v);
+        if (const char* v = std::getenv("TOMO_FWD_ROWS")) c->rows_fwd = std::atoi(v);
         if (const char* v = std::getenv("TOMO_ADJ_PAIR")) c->adj_pair = std::atoi(v) != 0;
         if (const char* v = std::getenv("TOMO_ADJ_PAIR_ROWS")) c->rows_adj2 = std::atoi(v);
         if (const char* v = std::getenv("TOMO_FWD_PAIR")) c->fwd_pair = std::atoi(v) != 0 && c->S >= 4;
@@ -319,6 +320,22 @@ tomo_status autotune(tomo_ctx* c) {
             if (tlog) std::fprintf(stderr, "tomo tune: adjoint pair code %d %.2f us/step\n", code, 1e3 * ms / reps);
             if (ms < best_a) { best_a = ms; c->rows_adj2 = code; c->adj_pair = true; }
         }
+    }
+    // one-step forward with its inputs staged in shared memory
+    for (int code : {3204, 3208, 3216, 3304, 3308, 3316}) {
+        if (code % 100 > 4 * c->geo.ny) continue;
+        float ms = 1e30f;
+        for (int pass = 0; pass < passes; ++pass) {
+            CU(c, cudaEventRecord(c->ev0, c->st));
+            for (int t = 0; t < reps; ++t) launch_fwd_strip(code, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), c->st);
+            CU(c, cudaEventRecord(c->ev1, c->st));
+            CU(c, cudaEventSynchronize(c->ev1));
+            float t_ms = 0.f;
+            CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+            if (pass > 0) ms = std::min(ms, t_ms);
+        }
+        if (tlog) std::fprintf(stderr, "tomo tune: forward staged code %d %.2f us/step\n", code, 1e3 * ms / reps);
+        if (ms < best_f1) { best_f1 = ms; rows_f1 = code; }
     }
     // A two-step forward must win clearly: inside a sweep it also carries the odd leftover step,
     // the sensor gather of two slices and the checkpoint copies, which the trial does not time.

@@ -1238,6 +1238,121 @@ void fwd2_strip(const DevGeo& g, const float* coef, const Fwd2Step& s, cudaStrea
     k_fwd2_strip<R><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
 }
 
+// One forward step per launch with the row inputs staged in shared memory: a per-warp ring of
+// D rows of u(k) (row j+1, with one 4-cell chunk of halo on each side), u(k-1) and the
+// coefficient (row j), filled by 16-byte cp.async copies D rows ahead.  The west/east
+// neighbours of every lane come from the staged halo row, so lanes 0 and 31 make no extra
+// global loads.  Same arithmetic and sensor gather as k_fwd_strip: identical results.
+constexpr int F1_UC = STRIP + 8;                 // u(k) row with halo: cells x0-4 .. x0+131
+constexpr int F1_ROW = F1_UC + 2 * STRIP;        // + u(k-1) row + coefficient row
+
+template <int R, int D>
+__global__ void __launch_bounds__(WARPS * 32, 8) k_fwds_strip(DevGeo g, const float* __restrict__ coef, FwdStep s) {
+    extern __shared__ float4 f1_mem4[];
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    if (blockIdx.y == gridDim.y - 1) {
+        // sensor gather of slice k (k >= 2), one block per group
+        if (blockIdx.x != 0 || s.gk < 2) return;
+        const float* u = s.uc + gl * s.gstride;
+        const int64_t base = ((int64_t)gl * g.nt + s.gk) * g.nch;
+        const bool noisy = s.gmeas && g.noise_key;
+        const uint64_t key = noisy ? *g.noise_key : 0;
+        for (int c = threadIdx.x; c < g.nch; c += blockDim.x) {
+            const int cell = g.rcv[c];
+            float v = cell >= 0 ? u[cell] : 0.f;
+            if (noisy) v *= noise_factor(key, g.noise_level, s.g0 + gl, s.gk, c);
+            s.gout[base + c] = s.gmeas ? (cell >= 0 ? s.gmeas[base + c] - v : 0.f) : v;
+        }
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * STRIP;
+    const int i = x0 + 4 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    float* ring = reinterpret_cast<float*>(f1_mem4) + warp * D * F1_ROW;
+    const bool act = i < nx;
+    const float* uc = s.uc + gl * s.gstride;
+    const float* up = s.up + gl * s.gstride;
+    float* un = s.un + gl * s.gstride;
+    float* ck = s.ck ? s.ck + gl * s.ckstride : nullptr;
+    const bool edge_x = x0 < g.sponge_w || x0 + STRIP > nx - g.sponge_w;
+    const bool src = s.k < g.n_src_steps;
+    const int32_t* em = g.emit + (int64_t)(s.g0 + gl) * g.gs;
+    const float a = src ? g.src[s.k] : 0.f;
+    const int jend = min(y0 + R, ny);
+    // copy duty: u(k) chunks lane (and 32 + lane for lanes 0, 1), u(k-1) and coefficient chunk lane
+    const int cxu = x0 - 4 + 4 * lane, cxu2 = x0 + 124 + 4 * lane, cx = x0 + 4 * lane;
+    const bool oku = cxu >= 0 && cxu + 3 < nx, oku2 = lane < 2 && cxu2 >= 0 && cxu2 + 3 < nx;
+    const bool okc = cx + 3 < nx;
+    const unsigned ring_s = (unsigned)__cvta_generic_to_shared(ring);
+    auto stage = [&](int t, int slot) {              // row t: u(k) row t+1, u(k-1) and coefficient row t
+        const unsigned dst = ring_s + 4u * (unsigned)(slot * F1_ROW);
+        const bool r1 = t + 1 < ny, r0 = t < ny;     // t >= y0 >= 0
+        const int o1 = (t + 1) * nx, o0 = t * nx;
+        cp_async16(dst + 16u * lane, uc + (r1 && oku ? o1 + cxu : 0), r1 && oku);
+        if (lane < 2) cp_async16(dst + 16u * (32 + lane), uc + (r1 && oku2 ? o1 + cxu2 : 0), r1 && oku2);
+        cp_async16(dst + 4u * F1_UC + 16u * lane, up + (r0 && okc ? o0 + cx : 0), r0 && okc);
+        cp_async16(dst + 4u * (F1_UC + STRIP) + 16u * lane, coef + (r0 && okc ? o0 + cx : 0), r0 && okc);
+    };
+    // rows y0-1 and y0 of u(k) and the neighbours of row y0 straight from global memory
+    float4 rm = ld4(uc, (y0 - 1) * nx + i, act && y0 > 0);
+    float4 r0 = ld4(uc, y0 * nx + i, act);
+    float w0, e0;
+    we(r0, uc + y0 * nx, lane, x0, nx, w0, e0);
+#pragma unroll
+    for (int t = 0; t < D; ++t) {
+        if (y0 + t < jend) stage(y0 + t, t);
+        cp_async_commit();
+    }
+    int slot = 0;
+#pragma unroll 1
+    for (int j = y0; j < jend; ++j) {
+        const int row = j * nx;
+        cp_async_wait<D - 1>();
+        __syncwarp();
+        const float* sr = ring + slot * F1_ROW;
+        const float4 rp = *reinterpret_cast<const float4*>(sr + 4 + 4 * lane);
+        const float wp = sr[3 + 4 * lane], ep = sr[8 + 4 * lane];     // neighbours of row j+1
+        const float4 p = *reinterpret_cast<const float4*>(sr + F1_UC + 4 * lane);
+        const float4 c = *reinterpret_cast<const float4*>(sr + F1_UC + STRIP + 4 * lane);
+        __syncwarp();
+        if (j + D < jend) stage(j + D, slot);
+        cp_async_commit();
+        slot = slot + 1 == D ? 0 : slot + 1;
+        const bool near = edge_x || j < g.sponge_w || j >= ny - g.sponge_w;
+        const float dx = near ? sponge(g, i, j) : 1.f;
+        const float dy = near ? sponge(g, i + 1, j) : 1.f;
+        const float dz = near ? sponge(g, i + 2, j) : 1.f;
+        const float dw = near ? sponge(g, i + 3, j) : 1.f;
+        const int64_t q0 = row + i;
+        const float ax = src ? emit_at(em, g.gs, q0, a) : 0.f;
+        const float ay = src ? emit_at(em, g.gs, q0 + 1, a) : 0.f;
+        const float az = src ? emit_at(em, g.gs, q0 + 2, a) : 0.f;
+        const float aw = src ? emit_at(em, g.gs, q0 + 3, a) : 0.f;
+        float4 v;
+        v.x = fwd_cell(r0.y, w0, rm.x, rp.x, r0.x, p.x, c.x, dx, ax);
+        v.y = fwd_cell(r0.z, r0.x, rm.y, rp.y, r0.y, p.y, c.y, dy, ay);
+        v.z = fwd_cell(r0.w, r0.y, rm.z, rp.z, r0.z, p.z, c.z, dz, az);
+        v.w = fwd_cell(e0, r0.z, rm.w, rp.w, r0.w, p.w, c.w, dw, aw);
+        if (act) {
+            *reinterpret_cast<float4*>(un + row + i) = v;
+            if (ck) *reinterpret_cast<float4*>(ck + row + i) = v;
+        }
+        rm = r0; r0 = rp; w0 = wp; e0 = ep;
+    }
+    cp_async_wait<0>();
+}
+
+template <int R, int D>
+void fwds_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    const size_t smem = sizeof(float) * WARPS * D * F1_ROW;
+    dim3 grid((g.nx + STRIP - 1) / STRIP, (g.ny + rows_per_block - 1) / rows_per_block + 1, s.ng);
+    k_fwds_strip<R, D><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
+}
+
 template <int R>
 void fwd_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
@@ -1350,7 +1465,13 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
 
 void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& s, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
-    switch (rows) {
+    switch (rows) {   // 3000 + 100 D + rows: inputs staged in shared memory D rows ahead
+    case 3204: fwds_strip<4, 2>(g, coef, s, st); break;
+    case 3208: fwds_strip<8, 2>(g, coef, s, st); break;
+    case 3216: fwds_strip<16, 2>(g, coef, s, st); break;
+    case 3304: fwds_strip<4, 3>(g, coef, s, st); break;
+    case 3308: fwds_strip<8, 3>(g, coef, s, st); break;
+    case 3316: fwds_strip<16, 3>(g, coef, s, st); break;
     case 2: fwd_strip<2>(g, coef, s, st); break;
     case 4: fwd_strip<4>(g, coef, s, st); break;
     case 16: fwd_strip<16>(g, coef, s, st); break;
