@@ -758,6 +758,11 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
     const bool edge_x = x0 < g.sponge_w || x0 + 64 > nx - g.sponge_w;
     auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
     const RcvMask rk = rcv_mask(g, x0, x0 + 64);
+    // receiver flags of the warp's rows y0-1 .. y0+R (R + 2 <= 64): lane l tests rows y0-1+l and
+    // y0+31+l, one ballot each, so the row loop reads a bit instead of the bitmap
+    const unsigned rb_lo = __ballot_sync(FULL, rcv_row(g, rk, y0 - 1 + lane));
+    const unsigned rb_hi = R + 2 > 32 ? __ballot_sync(FULL, rcv_row(g, rk, y0 + 31 + lane)) : 0u;
+    const unsigned long long rbits = ((unsigned long long)rb_hi << 32) | rb_lo;
     const int dca = edge_dist(i, nx), dcb = edge_dist(i + 1, nx);
     // copy duty of this lane: chunk (lane & 15) of arrays 2*slot + (lane >> 4), slot 0..2
     const int ch = lane & 15, half = lane >> 4;
@@ -814,7 +819,7 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
         if (r + D <= rlast) stage(r + D, slot);
         cp_async_commit();
         slot = slot + 1 == D ? 0 : slot + 1;
-        const bool rcv = rcv_row(g, rk, r);
+        const bool rcv = (rbits >> (r - y0 + 1)) & 1ull;
         int2 rid = make_int2(-1, -1);
         if (rcv && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
         const float2 pzp = mul2(cp, z1p);
