@@ -756,6 +756,8 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
     const float* rrb = s.rrb + gl * s.rrstride;
     float* corr = s.corr + gl * s.cstride;
     const bool edge_x = x0 < g.sponge_w || x0 + 64 > nx - g.sponge_w;
+    // any row y0-1 .. y0+R inside the sponge: only then do rows need the sponge table
+    const bool damp_any = edge_x || y0 - 1 < g.sponge_w || y0 + R >= ny - g.sponge_w;
     auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
     const RcvMask rk = rcv_mask(g, x0, x0 + 64);
     // receiver flags of the warp's rows y0-1 .. y0+R (R + 2 <= 64): lane l tests rows y0-1+l and
@@ -827,10 +829,13 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
         {
             const float pw = __shfl_up_sync(FULL, pz0.y, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
             if (ok) {
-                const int dr = edge_dist(r, ny);
-                const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
-                float dx = drow, dy = drow;
-                if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+                float dx = 1.f, dy = 1.f;
+                if (damp_any) {
+                    const int dr = edge_dist(r, ny);
+                    const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+                    dx = drow; dy = drow;
+                    if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+                }
                 float ix = 0.f, iy = 0.f;
                 if (rcv) {
                     ix = rid.x >= 0 ? rra[rid.x] : 0.f;
@@ -848,10 +853,13 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
             const float ubw = __shfl_up_sync(FULL, ubm.y, 1), ube = __shfl_down_sync(FULL, ubm.x, 1);
             if (own && rb >= y0 && rb < ny) {
                 const int rowb = rb * nx;
-                const int dr = edge_dist(rb, ny);
-                const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
-                float dx = drow, dy = drow;
-                if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+                float dx = 1.f, dy = 1.f;
+                if (damp_any) {
+                    const int dr = edge_dist(rb, ny);
+                    const float drow = dr < g.sponge_w ? g.damp[dr] : 1.f;
+                    dx = drow; dy = drow;
+                    if (edge_x) { dx = damp_at(g, dca, dr); dy = damp_at(g, dcb, dr); }
+                }
                 float ix = 0.f, iy = 0.f;
                 if (rcvm) {
                     ix = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
