@@ -57,6 +57,16 @@ def test_phantom_matches_oracle(built_lib):
     assert e.std() > 0.005
 
 
+def test_host_allocation_failure_is_a_status(built_lib):
+    # a 2^30 x 2^30 phantom needs a host buffer larger than the address space: the C++
+    # exception below the entry point comes back as a status (nothing is written to fo)
+    fo = np.zeros(4, np.float32)
+    st = built_lib.tomo_phantom_cfg(1 << 30, 1 << 30, 1, 0, 10.0, 20.0, 0.1, 0.0, 50.0, 1,
+                                    fo.ctypes.data_as(C.POINTER(C.c_float)))
+    assert st == tomo.ERR_OOM
+    assert not fo.any()
+
+
 def test_bad_config_rejected_before_device(built_lib):
     for bad in (tomo.ref_config(ring_lo=1), tomo.ref_config(ring_hi=190), tomo.ref_config(group_size=0),
                 tomo.cfg_config(radius=70.0), tomo.cfg_config(courant=0.9)):

@@ -173,8 +173,8 @@ struct LoopOpts {
     const char* conv_name;   // sirt_convergence.txt / art_convergence.txt
     const char* time_name;
     // optional per-iteration method and schedule (hybrid and alternating drivers)
-    std::function<int(int)> method_at;
-    std::function<tomo_schedule(int)> sched_at;
+    std::function<int(int)> method_at = {};
+    std::function<tomo_schedule(int)> sched_at = {};
 };
 
 // The iteration loop with the reference's stopping rule and log files.

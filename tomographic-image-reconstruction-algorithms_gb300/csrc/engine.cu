@@ -25,6 +25,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <memory>
 #include <string>
 #include <tuple>
 #include <thread>
@@ -100,16 +101,16 @@ struct tomo_ctx {
     }
     template <typename T>
     tomo_status alloc(T** p, int64_t n, const char* what) {
-        void* q = nullptr;
         const size_t b = (size_t)std::max<int64_t>(n, 1) * sizeof(T);
-        const cudaError_t e = cudaMalloc(&q, b);
+        allocs.push_back(nullptr);   // the slot first: a push_back that throws leaks no device memory
+        const cudaError_t e = cudaMalloc(&allocs.back(), b);
         if (e != cudaSuccess) {
+            allocs.pop_back();
             cudaGetLastError();
             return fail(TOMO_ERR_OOM, "cudaMalloc(%s, %zu bytes): %s", what, b, cudaGetErrorString(e));
         }
-        allocs.push_back(q);
         bytes += (int64_t)b;
-        *p = (T*)q;
+        *p = (T*)allocs.back();
         return TOMO_OK;
     }
     // residual noise (tomo_set_residual_noise): kind 0 off, 2 a fresh draw per gradient sweep,
@@ -465,7 +466,6 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     const int nt = g.nt, S = c->S, K = c->K;
     const int64_t N = g.N, gstride = (int64_t)S * N, nch = g.nch, rpg = c->recs_per_group();
     void* st = c->st;
-    const int prof = g.cfg.profile;
     // ---- forward sweep
     launch_zero_slots(c->hist, ng, gstride, c->slot(0), c->slot(1), N, st);
     ++n;
@@ -882,6 +882,8 @@ tomo_status features_core(tomo_ctx* c, double* r2) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// C entry points.  Those that can allocate on the host are function-try-blocks: a C++
+// exception below them becomes a status (abi_exception) and never crosses the C ABI.
 extern "C" {
 
 int32_t tomo_abi_version(void) { return TOMO_ABI_VERSION; }
@@ -921,37 +923,37 @@ tomo_status tomo_config_init(tomo_config* cfg, int32_t profile) {
     return TOMO_OK;
 }
 
-tomo_status tomo_create(const tomo_config* cfg, tomo_ctx** out) {
+tomo_status tomo_create(const tomo_config* cfg, tomo_ctx** out) try {
     g_create_error.clear();
     if (!cfg || !out) { g_create_error = "NULL argument"; return TOMO_ERR_ARG; }
     *out = nullptr;
-    tomo_ctx* c = new (std::nothrow) tomo_ctx();
+    std::unique_ptr<tomo_ctx> c(new (std::nothrow) tomo_ctx());   // freed on every early return
     if (!c) return TOMO_ERR_OOM;
     c->dev = -1;
     std::string why;
     tomo_status s = build_geometry(*cfg, c->geo, why);
-    if (s != TOMO_OK) { g_create_error = why; delete c; return s; }
+    if (s != TOMO_OK) { g_create_error = why; return s; }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();
         g_create_error = "no CUDA device";
-        delete c;
         return TOMO_ERR_CUDA;
     }
-    if (cfg->device < 0 || cfg->device >= ndev) { g_create_error = "device ordinal out of range"; delete c; return TOMO_ERR_ARG; }
+    if (cfg->device < 0 || cfg->device >= ndev) { g_create_error = "device ordinal out of range"; return TOMO_ERR_ARG; }
     c->dev = cfg->device;
     if ((s = c->cuda(cudaSetDevice(c->dev), "cudaSetDevice")) == TOMO_OK &&
         (s = c->cuda(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate")) == TOMO_OK &&
         (s = c->cuda(cudaEventCreate(&c->ev0), "cudaEventCreate")) == TOMO_OK &&
-        (s = c->cuda(cudaEventCreate(&c->ev1), "cudaEventCreate")) == TOMO_OK && (s = make_plan(c)) == TOMO_OK)
-        s = create_buffers(c);
+        (s = c->cuda(cudaEventCreate(&c->ev1), "cudaEventCreate")) == TOMO_OK && (s = make_plan(c.get())) == TOMO_OK)
+        s = create_buffers(c.get());
     if (s != TOMO_OK) {
         g_create_error = c->err;
-        delete c;
         return s;
     }
-    *out = c;
+    *out = c.release();
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(&g_create_error);
 }
 
 void tomo_destroy(tomo_ctx* ctx) { delete ctx; }
@@ -979,14 +981,20 @@ tomo_status tomo_transducers(const tomo_ctx* c, int32_t* ii, int32_t* jj) {
     return TOMO_OK;
 }
 
-tomo_status tomo_phantom_ref(int32_t nx, int32_t ny, float* fo) { return phantom_ref(nx, ny, fo); }
-
-tomo_status tomo_phantom_cfg(int32_t nx, int32_t ny, int32_t kind, int32_t n, float rmin, float rmax, float vmax,
-                             float noise_sigma, float support, uint64_t seed, float* fo) {
-    return phantom_cfg(nx, ny, kind, n, rmin, rmax, vmax, noise_sigma, support, seed, fo);
+tomo_status tomo_phantom_ref(int32_t nx, int32_t ny, float* fo) try {
+    return phantom_ref(nx, ny, fo);
+} catch (...) {
+    return abi_exception(nullptr);
 }
 
-tomo_status tomo_forward(tomo_ctx* c, const float* f, float* records, float* u_last) {
+tomo_status tomo_phantom_cfg(int32_t nx, int32_t ny, int32_t kind, int32_t n, float rmin, float rmax, float vmax,
+                             float noise_sigma, float support, uint64_t seed, float* fo) try {
+    return phantom_cfg(nx, ny, kind, n, rmin, rmax, vmax, noise_sigma, support, seed, fo);
+} catch (...) {
+    return abi_exception(nullptr);
+}
+
+tomo_status tomo_forward(tomo_ctx* c, const float* f, float* records, float* u_last) try {
     if (!c || !f || !records) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
     const Geometry& g = c->geo;
@@ -997,9 +1005,11 @@ tomo_status tomo_forward(tomo_ctx* c, const float* f, float* records, float* u_l
     CU(c, cudaStreamSynchronize(c->st));
     CU(c, cudaGetLastError());
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
-tomo_status tomo_generate_data(tomo_ctx* c, const float* f_true, float* records, const tomo_noise* noise) {
+tomo_status tomo_generate_data(tomo_ctx* c, const float* f_true, float* records, const tomo_noise* noise) try {
     TRY(tomo_forward(c, f_true, records, nullptr));
     if (noise && noise->kind == 1 && noise->level > 0.f)
         add_record_noise(records, c->geo.G, c->geo.nt, c->geo.nch, noise->level, noise->seed);
@@ -1008,9 +1018,11 @@ tomo_status tomo_generate_data(tomo_ctx* c, const float* f_true, float* records,
     else if (noise && (noise->kind < 0 || noise->kind > 3))
         return c->fail(TOMO_ERR_ARG, "unknown noise kind %d", noise->kind);
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
-tomo_status tomo_set_residual_noise(tomo_ctx* c, const tomo_noise* noise) {
+tomo_status tomo_set_residual_noise(tomo_ctx* c, const tomo_noise* noise) try {
     if (!c) return TOMO_ERR_ARG;
     const int kind = noise ? noise->kind : 0;
     if (kind != 0 && kind != 2 && kind != 3) return c->fail(TOMO_ERR_ARG, "residual noise kind must be 0, 2 or 3");
@@ -1030,9 +1042,11 @@ tomo_status tomo_set_residual_noise(tomo_ctx* c, const tomo_noise* noise) {
     c->drop_graphs();                       // captured launches hold the old DevGeo
     CU(c, cudaStreamSynchronize(c->st));
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
-tomo_status tomo_set_records(tomo_ctx* c, const float* records) {
+tomo_status tomo_set_records(tomo_ctx* c, const float* records) try {
     if (!c || !records) return c ? c->fail(TOMO_ERR_ARG, "NULL records") : TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
     CU(c, cudaMemcpyAsync(c->meas, records, sizeof(float) * (size_t)c->geo.G * c->recs_per_group(),
@@ -1040,10 +1054,12 @@ tomo_status tomo_set_records(tomo_ctx* c, const float* records) {
     CU(c, cudaStreamSynchronize(c->st));
     c->meas_set = true;
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 tomo_status tomo_gradient(tomo_ctx* c, const float* f, const float* records, float* dfg, float* df,
-                          double* resid_norm2) {
+                          double* resid_norm2) try {
     if (!c || !f) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
     if (records) TRY(tomo_set_records(c, records));
     if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
@@ -1066,10 +1082,12 @@ tomo_status tomo_gradient(tomo_ctx* c, const float* f, const float* records, flo
     CU(c, cudaStreamSynchronize(c->st));
     CU(c, cudaGetLastError());
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 tomo_status tomo_iterate(tomo_ctx* c, int32_t method, const tomo_schedule* sched, int32_t iter, float* f_inout,
-                         const float* records, const float* f_true, tomo_iter_stats* stats) {
+                         const float* records, const float* f_true, tomo_iter_stats* stats) try {
     if (!c || !f_inout) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
     if (records) TRY(tomo_set_records(c, records));
@@ -1081,11 +1099,13 @@ tomo_status tomo_iterate(tomo_ctx* c, int32_t method, const tomo_schedule* sched
     CU(c, cudaMemcpyAsync(f_inout, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToHost, c->st));
     CU(c, cudaStreamSynchronize(c->st));
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 tomo_status tomo_run(tomo_ctx* c, int32_t method, const tomo_schedule* sched, float* f_inout, const float* records,
                      const float* f_true, float target_epsilon, int32_t max_iters, double* eps_log,
-                     int32_t* iters_done) {
+                     int32_t* iters_done) try {
     if (!c || !f_inout || !f_true) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
     if (records) TRY(tomo_set_records(c, records));
@@ -1111,9 +1131,11 @@ tomo_status tomo_run(tomo_ctx* c, int32_t method, const tomo_schedule* sched, fl
     if (iters_done) *iters_done = done;
     if (result == TOMO_ERR_DIVERGED) c->err = "epsilon rose or became NaN";
     return result;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
-tomo_status tomo_forward_device(tomo_ctx* c, const float* d_f, float* d_records) {
+tomo_status tomo_forward_device(tomo_ctx* c, const float* d_f, float* d_records) try {
     if (!c || !d_f || !d_records) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
     const Geometry& g = c->geo;
@@ -1122,10 +1144,12 @@ tomo_status tomo_forward_device(tomo_ctx* c, const float* d_f, float* d_records)
     CU(c, cudaMemcpyAsync(d_records, c->rec, sizeof(float) * (size_t)g.G * c->recs_per_group(),
                           cudaMemcpyDeviceToDevice, c->st));
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 tomo_status tomo_iterate_device(tomo_ctx* c, int32_t method, const tomo_schedule* sched, int32_t iter, float* d_f,
-                                const float* d_records, const float* d_f_true, tomo_iter_stats* stats) {
+                                const float* d_records, const float* d_f_true, tomo_iter_stats* stats) try {
     if (!c || !d_f) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
     const Geometry& g = c->geo;
@@ -1140,9 +1164,11 @@ tomo_status tomo_iterate_device(tomo_ctx* c, int32_t method, const tomo_schedule
     TRY(iterate_core(c, method, sched, iter, d_f_true != nullptr, stats));
     CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
-tomo_status tomo_features_device(tomo_ctx* c, const float* d_f, float* d_feat, double* resid_norm2) {
+tomo_status tomo_features_device(tomo_ctx* c, const float* d_f, float* d_feat, double* resid_norm2) try {
     if (!c || !d_f || !d_feat) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
     if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
     CU(c, cudaSetDevice(c->dev));
@@ -1154,10 +1180,12 @@ tomo_status tomo_features_device(tomo_ctx* c, const float* d_f, float* d_feat, d
     CU(c, cudaStreamSynchronize(c->st));
     if (resid_norm2) *resid_norm2 = r2;
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fallback, int32_t iter, float* d_f,
-                                 const float* d_f_true, tomo_iter_stats* stats, int32_t* accepted) {
+                                 const float* d_f_true, tomo_iter_stats* stats, int32_t* accepted) try {
     if (!c || !net || !fallback || !d_f) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
     if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
     CU(c, cudaSetDevice(c->dev));
@@ -1207,12 +1235,14 @@ tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule
         stats->kernel_launches = (double)(c->launches - launches0);
     }
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fallback, float* d_f,
                              const float* d_f_true, double target_epsilon, int32_t max_iters, double min_decrease,
                              int32_t patience, double* eps_log, int32_t* step_log, int32_t* iters_done,
-                             int32_t* sweeps, double* seconds) {
+                             int32_t* sweeps, double* seconds) try {
     if (!c || !net || !fallback || !d_f || max_iters < 0 || !(min_decrease >= 0.0 && min_decrease < 1.0) ||
         patience < 0)
         return c ? c->fail(TOMO_ERR_ARG, "bad tomo_run_learned arguments") : TOMO_ERR_ARG;
@@ -1275,16 +1305,19 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
     if (sweeps) *sweeps = nsweep;
     if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* ms_per_launch,
-                             double* bytes_per_launch) {
+                             double* bytes_per_launch) try {
     if (!c || (which != 0 && which != 1) || steps < 1 || !ms_per_launch)
         return c ? c->fail(TOMO_ERR_ARG, "bad tomo_time_kernel arguments") : TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
     const Geometry& g = c->geo;
     const int nt = g.nt, ng = c->P, prof = g.cfg.profile;
     const int64_t N = g.N;
+    if (nt < 5) return c->fail(TOMO_ERR_ARG, "tomo_time_kernel needs nt >= 5");
     steps = std::min(steps, nt - 4);
     const int k0 = std::max(2, (nt - steps) / 2);
     launch_coef(prof, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
@@ -1315,11 +1348,13 @@ tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* 
     *ms_per_launch = (double)ms / steps;
     if (bytes_per_launch) *bytes_per_launch = (which == 0 ? 16.0 : 20.0) * (double)ng * (double)N;
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const tomo_schedule* sched,
                                int32_t iter0, int32_t iters, float** d_f, const float** d_f_true, double* eps_log,
-                               double* seconds) {
+                               double* seconds) try {
     if (!ctxs || n < 1 || !sched || !d_f || iters < 0) return TOMO_ERR_ARG;
     for (int i = 0; i < n; ++i) {
         if (!ctxs[i] || !d_f[i]) return TOMO_ERR_ARG;
@@ -1327,34 +1362,44 @@ tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const
             if (ctxs[j] == ctxs[i]) return ctxs[i]->fail(TOMO_ERR_ARG, "a context appears twice in the batch");
     }
     std::vector<tomo_status> st(n, TOMO_OK);
+    auto work = [&](int i) noexcept {   // the entry points it calls catch their own exceptions
+        const float* ft = d_f_true ? d_f_true[i] : nullptr;
+        for (int it = 0; it < iters && st[i] == TOMO_OK; ++it) {
+            tomo_iter_stats s{};
+            st[i] = tomo_iterate_device(ctxs[i], method, sched, iter0 + it, d_f[i], nullptr, ft, &s);
+            if (eps_log) eps_log[(int64_t)i * iters + it] = s.epsilon;
+        }
+        if (st[i] == TOMO_OK) st[i] = tomo_synchronize(ctxs[i]);
+    };
     const auto t0 = std::chrono::steady_clock::now();
     {
         std::vector<std::thread> pool;
         pool.reserve(n);
-        for (int i = 0; i < n; ++i)
-            pool.emplace_back([&, i] {
-                const float* ft = d_f_true ? d_f_true[i] : nullptr;
-                for (int it = 0; it < iters && st[i] == TOMO_OK; ++it) {
-                    tomo_iter_stats s{};
-                    st[i] = tomo_iterate_device(ctxs[i], method, sched, iter0 + it, d_f[i], nullptr, ft, &s);
-                    if (eps_log) eps_log[(int64_t)i * iters + it] = s.epsilon;
-                }
-                if (st[i] == TOMO_OK) st[i] = tomo_synchronize(ctxs[i]);
-            });
+        for (int i = 0; i < n; ++i) {
+            try {
+                pool.emplace_back(work, i);
+            } catch (...) {
+                work(i);   // no thread to be had: this context runs on the calling thread
+            }
+        }
         for (auto& t : pool) t.join();
     }
     if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (int i = 0; i < n; ++i)
         if (st[i] != TOMO_OK) return st[i];
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(nullptr);
 }
 
-tomo_status tomo_synchronize(tomo_ctx* c) {
+tomo_status tomo_synchronize(tomo_ctx* c) try {
     if (!c) return TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
     CU(c, cudaStreamSynchronize(c->st));
     CU(c, cudaGetLastError());
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
 }
 
 }  // extern "C"

@@ -2,6 +2,9 @@
 #pragma once
 
 #include <cstdint>
+#include <exception>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -29,6 +32,36 @@ TOMO_HD inline float noise_uniform(uint64_t key, int g, int k, int c) {
 // Multiplicative record noise factor 1 + level (2U - 1).
 TOMO_HD inline float noise_factor(uint64_t key, float level, int g, int k, int c) {
     return 1.0f + level * (2.0f * noise_uniform(key, g, k, c) - 1.0f);
+}
+
+// Status for the C++ exception in flight (host allocation or thread creation failure), its
+// message into *err.  The C entry points are function-try-blocks whose handler returns this, so
+// no exception crosses the C ABI.  Call only from inside a catch handler.
+inline tomo_status abi_exception(std::string* err) noexcept {
+    tomo_status s = TOMO_ERR_STATE;
+    const char* why = "unknown C++ exception";
+    std::string what;
+    try {
+        throw;
+    } catch (const std::bad_alloc&) {
+        s = TOMO_ERR_OOM;
+        why = "host memory allocation failed";
+    } catch (const std::length_error&) {
+        s = TOMO_ERR_OOM;
+        why = "host allocation larger than the address space";
+    } catch (const std::exception& e) {
+        why = "C++ exception";
+        try { what = e.what(); } catch (...) {}
+    } catch (...) {
+    }
+    if (err) {
+        try {
+            *err = why;
+            if (!what.empty()) *err += ": " + what;
+        } catch (...) {
+        }
+    }
+    return s;
 }
 
 // Reference constants (sirt-mimo.cu:26-35), the float values the reference uses.

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -74,13 +75,13 @@ struct tomo_net {
     }
     template <typename T>
     bool alloc(T** p, int64_t n) {
-        void* q = nullptr;
-        if (cudaMalloc(&q, sizeof(T) * (size_t)std::max<int64_t>(n, 1)) != cudaSuccess) {
+        allocs.push_back(nullptr);   // the slot first: a push_back that throws leaks no device memory
+        if (cudaMalloc(&allocs.back(), sizeof(T) * (size_t)std::max<int64_t>(n, 1)) != cudaSuccess) {
+            allocs.pop_back();
             cudaGetLastError();
             return false;
         }
-        allocs.push_back(q);
-        *p = (T*)q;
+        *p = (T*)allocs.back();
         return true;
     }
     tomo_status fail(tomo_status s, const std::string& why) {
@@ -185,19 +186,20 @@ tomo_status net_infer(tomo_net* n, const float* feat, int H, int W, float* out, 
 }  // namespace tomo
 
 // ---- C ABI -----------------------------------------------------------------------------
+// Entry points that can allocate on the host are function-try-blocks: a C++ exception below
+// them becomes a status (abi_exception) and never crosses the C ABI.
 extern "C" {
 
 int64_t tomo_net_num_params(void) { return kParams; }
 
-tomo_status tomo_net_create(int32_t device, uint64_t seed, tomo_net** out) {
+tomo_status tomo_net_create(int32_t device, uint64_t seed, tomo_net** out) try {
     if (!out) return TOMO_ERR_ARG;
     *out = nullptr;
-    tomo_net* n = new (std::nothrow) tomo_net();
+    std::unique_ptr<tomo_net> n(new (std::nothrow) tomo_net());   // freed on every early return
     if (!n) return TOMO_ERR_OOM;
     n->dev = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&n->st, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
-        delete n;
         return TOMO_ERR_CUDA;
     }
     bool ok = n->alloc(&n->w, kParams) && n->alloc(&n->g, kParams) && n->alloc(&n->m, kParams) &&
@@ -205,7 +207,7 @@ tomo_status tomo_net_create(int32_t device, uint64_t seed, tomo_net** out) {
     for (int l = 0; l < 3; ++l) ok = ok && n->alloc(&n->wf[l], kWmid) && n->alloc(&n->wd[l], kWmid);
     ok = ok && n->alloc(&n->part, (int64_t)kPartBlocks * (kWmid + C)) && n->alloc(&n->lpart, kPartBlocks) &&
          n->alloc(&n->ltot, 1);
-    if (!ok) { delete n; return TOMO_ERR_OOM; }
+    if (!ok) return TOMO_ERR_OOM;
     // He-normal initialisation for the ReLU layers, small output layer, zero biases
     std::vector<float> h(kParams, 0.f);
     Rng rng(seed);
@@ -221,27 +223,34 @@ tomo_status tomo_net_create(int32_t device, uint64_t seed, tomo_net** out) {
     fill(oW3, kWmid, 9.0 * C, 1.0, C, C);
     fill(oW4, kWmid, 9.0 * C, 1.0, C, C);
     for (int64_t e = 0; e < kW5; ++e) h[oW5 + e] = (float)(0.01 * std::sqrt(1.0 / (9.0 * C)) * rng.normal());
-    cudaMemcpy(n->w, h.data(), sizeof(float) * kParams, cudaMemcpyHostToDevice);
-    cudaMemset(n->m, 0, sizeof(float) * kParams);
-    cudaMemset(n->v, 0, sizeof(float) * kParams);
-    repack(n, n->st);
-    if (cudaStreamSynchronize(n->st) != cudaSuccess) { cudaGetLastError(); delete n; return TOMO_ERR_CUDA; }
-    *out = n;
+    if (cudaMemcpy(n->w, h.data(), sizeof(float) * kParams, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(n->m, 0, sizeof(float) * kParams) != cudaSuccess ||
+        cudaMemset(n->v, 0, sizeof(float) * kParams) != cudaSuccess) {
+        cudaGetLastError();
+        return TOMO_ERR_CUDA;
+    }
+    repack(n.get(), n->st);
+    if (cudaStreamSynchronize(n->st) != cudaSuccess) { cudaGetLastError(); return TOMO_ERR_CUDA; }
+    *out = n.release();
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(nullptr);
 }
 
 void tomo_net_destroy(tomo_net* n) { delete n; }
 
 const char* tomo_net_last_error(const tomo_net* n) { return n ? n->err.c_str() : ""; }
 
-tomo_status tomo_net_get_params(tomo_net* n, float* host) {
+tomo_status tomo_net_get_params(tomo_net* n, float* host) try {
     if (!n || !host) return TOMO_ERR_ARG;
     cudaSetDevice(n->dev);
     NCU(n, cudaMemcpy(host, n->w, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(n ? &n->err : nullptr);
 }
 
-tomo_status tomo_net_set_params(tomo_net* n, const float* host) {
+tomo_status tomo_net_set_params(tomo_net* n, const float* host) try {
     if (!n || !host) return TOMO_ERR_ARG;
     cudaSetDevice(n->dev);
     NCU(n, cudaMemcpy(n->w, host, sizeof(float) * kParams, cudaMemcpyHostToDevice));
@@ -251,9 +260,11 @@ tomo_status tomo_net_set_params(tomo_net* n, const float* host) {
     repack(n, n->st);
     NCU(n, cudaStreamSynchronize(n->st));
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(n ? &n->err : nullptr);
 }
 
-tomo_status tomo_net_forward_device(tomo_net* n, const float* d_feat, int32_t B, int32_t H, int32_t W, float* d_out) {
+tomo_status tomo_net_forward_device(tomo_net* n, const float* d_feat, int32_t B, int32_t H, int32_t W, float* d_out) try {
     if (!n || !d_feat || !d_out) return TOMO_ERR_ARG;
     cudaSetDevice(n->dev);
     tomo_status s = check_shape(n, B, H, W);
@@ -262,10 +273,12 @@ tomo_status tomo_net_forward_device(tomo_net* n, const float* d_feat, int32_t B,
     NCU(n, cudaStreamSynchronize(n->st));
     NCU(n, cudaGetLastError());
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(n ? &n->err : nullptr);
 }
 
 tomo_status tomo_net_grad_device(tomo_net* n, const float* d_feat, const float* d_target, const float* d_mask, int32_t B,
-                                 int32_t H, int32_t W, float* host_grad, double* loss) {
+                                 int32_t H, int32_t W, float* host_grad, double* loss) try {
     if (!n || !d_feat || !d_target || !d_mask) return TOMO_ERR_ARG;
     cudaSetDevice(n->dev);
     tomo_status s = check_shape(n, B, H, W);
@@ -273,10 +286,12 @@ tomo_status tomo_net_grad_device(tomo_net* n, const float* d_feat, const float* 
     if ((s = backward(n, d_feat, d_target, d_mask, B, H, W, loss)) != TOMO_OK) return s;
     if (host_grad) NCU(n, cudaMemcpy(host_grad, n->g, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(n ? &n->err : nullptr);
 }
 
 tomo_status tomo_net_train_step_device(tomo_net* n, const float* d_feat, const float* d_target, const float* d_mask,
-                                       int32_t B, int32_t H, int32_t W, float lr, double* loss) {
+                                       int32_t B, int32_t H, int32_t W, float lr, double* loss) try {
     if (!n || !d_feat || !d_target || !d_mask || !(lr > 0.f)) return TOMO_ERR_ARG;
     cudaSetDevice(n->dev);
     tomo_status s = check_shape(n, B, H, W);
@@ -291,9 +306,11 @@ tomo_status tomo_net_train_step_device(tomo_net* n, const float* d_feat, const f
     NCU(n, cudaStreamSynchronize(n->st));
     NCU(n, cudaGetLastError());
     return TOMO_OK;
+} catch (...) {
+    return abi_exception(n ? &n->err : nullptr);
 }
 
-tomo_status tomo_net_save(tomo_net* n, const char* path) {
+tomo_status tomo_net_save(tomo_net* n, const char* path) try {
     if (!n || !path) return TOMO_ERR_ARG;
     std::vector<float> h(kParams);
     tomo_status s = tomo_net_get_params(n, h.data());
@@ -306,21 +323,25 @@ tomo_status tomo_net_save(tomo_net* n, const char* path) {
               std::fwrite(h.data(), sizeof(float), h.size(), f) == h.size();
     ok = (std::fclose(f) == 0) && ok;
     return ok ? TOMO_OK : n->fail(TOMO_ERR_IO, "short write");
+} catch (...) {
+    return abi_exception(n ? &n->err : nullptr);
 }
 
-tomo_status tomo_net_load(tomo_net* n, const char* path) {
+tomo_status tomo_net_load(tomo_net* n, const char* path) try {
     if (!n || !path) return TOMO_ERR_ARG;
+    std::vector<float> h(kParams);   // before the file is opened: a throwing allocation leaks no FILE
     FILE* f = std::fopen(path, "rb");
     if (!f) return n->fail(TOMO_ERR_IO, std::string("cannot read ") + path);
     char magic[8];
     int64_t cnt = 0;
-    std::vector<float> h(kParams);
     const bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "TOMONET1", 8) == 0 &&
                     std::fread(&cnt, sizeof cnt, 1, f) == 1 && cnt == kParams &&
                     std::fread(h.data(), sizeof(float), h.size(), f) == h.size();
     std::fclose(f);
     if (!ok) return n->fail(TOMO_ERR_IO, "not a network parameter file");
     return tomo_net_set_params(n, h.data());
+} catch (...) {
+    return abi_exception(n ? &n->err : nullptr);
 }
 
 }  // extern "C"

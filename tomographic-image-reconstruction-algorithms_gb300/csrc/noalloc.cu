@@ -86,8 +86,9 @@ tomo_status scratch_address(unsigned char** out) {
 
 using namespace tomo;
 
+// A function-try-block: a C++ exception below it (host allocation failure) becomes a status.
 extern "C" tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float* d_f, float* d_records,
-                                            void* stream) {
+                                            void* stream) try {
     if (!cfg || !d_f || !d_records) return fail(TOMO_ERR_ARG, "NULL argument");
     Geometry geo;
     std::string why;
@@ -152,4 +153,9 @@ extern "C" tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float*
     NA_CU(cudaGetLastError());
 #undef NA_CU
     return TOMO_OK;
+} catch (...) {
+    std::string why;
+    const tomo_status s = abi_exception(&why);
+    std::fprintf(stderr, "tomo_forward_noalloc: %s\n", why.c_str());
+    return s;
 }
