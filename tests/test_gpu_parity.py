@@ -209,6 +209,44 @@ def test_checkpoint_and_passes_match_full_history(maker):
         assert r2 == ref_r2
 
 
+@pytest.mark.parametrize("maker,nx,ny", [(small_cfg, 70, 62), (small_ref, 63, 57)], ids=["cfg-70x62", "ref-63x57"])
+def test_per_cell_kernels_on_ragged_grids(maker, nx, ny):
+    """Grids whose width is not a multiple of 4 take the per-cell kernels (the warp-strip
+    kernels need nx % 4 == 0): records, gradients and two normalised SIRT iterations match
+    the oracle at the same tolerances."""
+    kw = dict(nx=nx, ny=ny) if maker is small_cfg else dict(nx=nx, ny=ny, ring_lo=8, ring_hi=48, group_size=20)
+    cfg = maker(**kw)
+    fo = blob_phantom(ny, nx, seed=41)
+    meas_o, ul_o = O.forward(cfg, fo.astype(np.float64), u_last=True)
+    f0 = blob_phantom(ny, nx, seed=42, amp=0.01)
+    dfg_o, r2_o = O.gradient(cfg, f0.astype(np.float64), meas_o)
+    tol_u, tol_r = field_tol(cfg, fo, ul_o, meas_o)
+    tol_g = TOL_GRAD
+    if cfg.profile == tomo.PROFILE_REF:
+        tol_g = max(TOL_GRAD, 3 * rel(O.gradient(cfg, f0.astype(np.float64), meas_o, prec=32)[0], dfg_o))
+    sched = (tomo.schedule(omega=0.02, normalize=1) if cfg.profile == tomo.PROFILE_CFG else
+             tomo.schedule(tomo.SCHED_POWER, omega=3e4, alpha=0.5, beta=0.5, gamma=1.5))
+    with tomo.Context(cfg) as ctx:
+        rec, ul = ctx.forward(fo, u_last=True)
+        assert rel(ul, ul_o) <= tol_u
+        assert rel(rec, meas_o) <= tol_r
+        dfg, _, r2 = ctx.gradient(f0, meas_o)
+        assert rel(dfg, dfg_o) <= tol_g
+        assert abs(r2 - r2_o) <= 1e-4 * r2_o
+        f = np.zeros_like(fo)
+        f_o = np.zeros(fo.shape, np.float64)
+        f_32 = np.zeros(fo.shape, np.float64)
+        for it in range(2):
+            st = ctx.iterate(tomo.SIRT_NORM, sched, it, f, None, fo)
+            eps_o = O.iterate(cfg, tomo.SIRT_NORM, sched, it, f_o, meas_o, fo.astype(np.float64))[0]
+            tol, tol_e = TOL_IMG, 1e-4 * eps_o
+            if cfg.profile == tomo.PROFILE_REF:
+                eps_32 = O.iterate(cfg, tomo.SIRT_NORM, sched, it, f_32, meas_o, fo.astype(np.float64), prec=32)[0]
+                tol, tol_e = max(TOL_IMG, 3 * rel(f_32, f_o)), max(tol_e, 3 * abs(eps_32 - eps_o))
+            assert rel(f, f_o) <= tol, (it, rel(f, f_o), tol)
+            assert abs(st.epsilon - eps_o) <= tol_e
+
+
 def test_run_stopping_rule():
     cfg = small_ref()
     fo = blob_phantom(cfg.ny, cfg.nx, seed=7)
