@@ -67,6 +67,57 @@ def test_host_allocation_failure_is_a_status(built_lib):
     assert not fo.any()
 
 
+def test_null_handles_are_statuses(built_lib):
+    """Every entry point answers a NULL context or network with TOMO_ERR_ARG (no device touched)."""
+    L = built_lib
+    sch = tomo.schedule(omega=1.0)
+    st = tomo.IterStats()
+    d = C.c_double()
+    i = C.c_int32()
+    calls = {
+        "tomo_forward": (None, None, None, None),
+        "tomo_generate_data": (None, None, None, None),
+        "tomo_set_records": (None, None),
+        "tomo_set_residual_noise": (None, None),
+        "tomo_gradient": (None, None, None, None, None, None),
+        "tomo_iterate": (None, 0, C.byref(sch), 0, None, None, None, C.byref(st)),
+        "tomo_run": (None, 0, C.byref(sch), None, None, None, 0.0, 1, None, None),
+        "tomo_forward_device": (None, None, None),
+        "tomo_iterate_device": (None, 0, C.byref(sch), 0, None, None, None, C.byref(st)),
+        "tomo_features_device": (None, None, None, None),
+        "tomo_iterate_learned": (None, None, C.byref(sch), 0, None, None, C.byref(st), C.byref(i)),
+        "tomo_run_learned": (None, None, C.byref(sch), None, None, 0.0, 1, 0.05, 2, None, None, None, None, None),
+        "tomo_time_kernel": (None, 0, 1, C.byref(d), None),
+        "tomo_iterate_batch": (None, 1, 0, C.byref(sch), 0, 1, None, None, None, None),
+        "tomo_synchronize": (None,),
+        "tomo_get_info": (None, None),
+        "tomo_transducers": (None, None, None),
+        "tomo_forward_noalloc": (None, None, None, None),
+        "tomo_net_get_params": (None, None),
+        "tomo_net_set_params": (None, None),
+        "tomo_net_save": (None, b"x"),
+        "tomo_net_load": (None, b"x"),
+        "tomo_net_forward_device": (None, None, 1, 8, 64, None),
+        "tomo_net_grad_device": (None, None, None, None, 1, 8, 64, None, None),
+        "tomo_net_train_step_device": (None, None, None, None, 1, 8, 64, 1e-3, None),
+    }
+    for name, args in calls.items():
+        assert getattr(L, name)(*args) == tomo.ERR_ARG, name
+    assert L.tomo_stream(None) is None
+    assert L.tomo_net_last_error(None) == b""
+    L.tomo_destroy(None)
+    L.tomo_net_destroy(None)
+
+
+def test_net_create_without_gpu_is_a_status(built_lib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert built_lib.tomo_net_create(0, 1, C.byref(h)) == tomo.ERR_CUDA and not h.value
+
+
 def test_bad_config_rejected_before_device(built_lib):
     for bad in (tomo.ref_config(ring_lo=1), tomo.ref_config(ring_hi=190), tomo.ref_config(group_size=0),
                 tomo.cfg_config(radius=70.0), tomo.cfg_config(courant=0.9)):
