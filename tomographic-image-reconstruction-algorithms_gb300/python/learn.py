@@ -1,7 +1,7 @@
 """Training and evaluation of the learned update (the 5-layer CNN in libtomo.so).
 
 Pipeline, all compute in libtomo.so's kernels (torch only holds device buffers):
-  1. data: seeded 256x256 ellipse phantoms (8 ellipses, axes 5..30 cells,
+  1. data: seeded 256x256 ellipse phantoms (8 ellipses, axes 8..45 cells,
      f in U[-0.15, 0.15], smoothed noise 0.01), the 512x512 workload's physics
      scaled to 256x256 (nt 1250, 128 transducers on radius 110, groups of 8,
      1% record noise).  Plain weighted SIRT (normalised-weight direction,
@@ -52,7 +52,7 @@ def phantom(cfg, seed, rmin, rmax):
     return tomo.phantom_cfg(cfg.nx, cfg.ny, 1, 8, rmin, rmax, 0.15, 0.01, 0.8 * cfg.radius, seed)
 
 
-TRAIN_RADII = (8.0, 45.0)   # ellipse semi-axes of the training phantoms (cells)
+TRAIN_RADII = (8.0, 45.0)   # range of the training ellipses' axes (diameters, cells)
 
 
 def mask_of(cfg):
