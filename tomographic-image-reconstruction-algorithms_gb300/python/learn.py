@@ -12,13 +12,16 @@ Pipeline, all compute in libtomo.so's kernels (torch only holds device buffers):
      6): the network learns to jump ahead along the plain trajectory.
   2. training: Adam on the masked mean squared error, on the GPU.
   3. evaluation (time to image): on the 512x512 workload, plain weighted SIRT
-     runs `plain_iters` iterations; the learned iteration (network proposal
-     accepted only when the record residual drops, else the plain step; see
+     runs `plain_iters` iterations; the learned iteration (a network proposal
+     is accepted only when it lowers the record residual by 5 %, else the plain
+     step is taken, and after 2 rejections in a row only plain steps; see
      tomo_run_learned) runs until it reaches the plain method's final image
      error.
 
 Usage:  python learn.py [--phantoms 400] [--iters 36] [--lookahead 6] [--epochs 12]
                         [--onpolicy-phantoms 200] [--out weights.bin]
+        (the defaults are the settings of the shipped weights/learned_update.bin:
+        12,400 pairs, network seed 7, data seeds 4000.., shuffling seed 0)
         python learn.py --eval-only --out weights.bin --eval-seeds 2001,2002
 """
 from __future__ import annotations
@@ -260,11 +263,11 @@ def time_to_image(net, plain_iters=30, seed=2001, device=0,
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--phantoms", type=int, default=1000)
+    ap.add_argument("--phantoms", type=int, default=400)
     ap.add_argument("--iters", type=int, default=36)
     ap.add_argument("--lookahead", type=int, default=6)
     ap.add_argument("--target", default="lookahead", choices=["lookahead", "truth"])
-    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default=WEIGHTS)
