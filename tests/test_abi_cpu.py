@@ -118,6 +118,46 @@ def test_net_create_without_gpu_is_a_status(built_lib):
     assert built_lib.tomo_net_create(0, 1, C.byref(h)) == tomo.ERR_CUDA and not h.value
 
 
+C_CLIENT = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "tomo.h"
+
+int main(void) {
+    tomo_config cfg;
+    if (tomo_config_init(&cfg, TOMO_PROFILE_REF) != TOMO_OK || cfg.nx != 192) return 1;
+    float* fo = (float*)calloc((size_t)cfg.nx * cfg.ny, sizeof(float));
+    if (!fo || tomo_phantom_ref(cfg.nx, cfg.ny, fo) != TOMO_OK) return 2;
+    int disc = 0;
+    for (int q = 0; q < cfg.nx * cfg.ny; ++q) disc += fo[q] > 0.f;
+    tomo_ctx* ctx = NULL;
+    cfg.group_size = 0;                                  /* invalid: rejected before any device call */
+    if (tomo_create(&cfg, &ctx) != TOMO_ERR_ARG || ctx != NULL) return 3;
+    printf("%d %d %s|%s\n", tomo_abi_version(), disc, tomo_status_string(TOMO_ERR_ARG), tomo_last_error(NULL));
+    free(fo);
+    return 0;
+}
+"""
+
+
+def test_header_is_c_and_links_from_c(built_lib, tmp_path):
+    """include/tomo.h compiles as strict C99 and a C program links against libtomo.so and runs
+    the host-side entry points."""
+    src = tmp_path / "client.c"
+    src.write_text(C_CLIENT)
+    exe = tmp_path / "client"
+    libdir = os.path.dirname(tomo.LIB_PATH)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I" + os.path.join(REPO, "include"),
+                        str(src), "-o", str(exe), "-L" + libdir, "-ltomo", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
+    ver, disc, rest = out.stdout.strip().split(" ", 2)
+    assert ver == "1" and int(disc) > 500
+    assert rest.startswith("invalid argument|") and len(rest) > len("invalid argument|")
+
+
 def test_bad_config_rejected_before_device(built_lib):
     for bad in (tomo.ref_config(ring_lo=1), tomo.ref_config(ring_hi=190), tomo.ref_config(group_size=0),
                 tomo.cfg_config(radius=70.0), tomo.cfg_config(courant=0.9)):
