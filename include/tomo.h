@@ -308,11 +308,16 @@ tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const
  * the records are valid once it completes.  The wavefield scratch lives in a
  * fixed file-scope device array of about 5.1 MiB that each GPU loading the
  * library holds until exit, so problems are limited to 512*512 cells, 2048
- * record channels, 2048 groups, 4096 emitters and 16384 time steps; larger ones
- * return TOMO_ERR_ARG with a one-line reason on stderr.  The first call on a
- * device looks the array's address up (cudaGetSymbolAddress); make that first
- * call before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race. */
+ * record channels and 16384 time steps (and 4096 emitters in the benchmark
+ * profile, 2048 groups in the reference profile); larger ones return
+ * TOMO_ERR_ARG with a one-line reason on stderr.  Each call looks the array's
+ * device address up in the current context (cudaGetSymbolAddress); the first
+ * call on a device also loads the library's device code there, so make that
+ * first call before any stream capture.  The geometry tables reach the array
+ * as kernel arguments, so no device work refers to host memory after the call
+ * returns.  All calls on a device share the one array: calls that overlap on
+ * the GPU (concurrent streams or threads) race, so serialise them on one
+ * stream. */
 tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float* d_f, float* d_records,
                                  void* stream);
 

@@ -5,10 +5,12 @@ owns all device memory, or latency-bound loops where an allocation would
 synchronise the device -- so this entry point runs the forward solve in a
 fixed device array compiled into libtomo.so and the caller's own buffers.
 These tests call it through the C ABI, twice in a row with different fields,
-and compare each result with the context-based tomo_forward, within the
-wavefield tolerance of the parity tests (1e-5 relative L2).  They also check
-that the second call leaves device free memory unchanged and that a problem
-beyond the array's limits is refused.
+on the legacy default stream and on a stream of their own, and compare each
+result with the context-based tomo_forward, within the wavefield tolerance of
+the parity tests (1e-5 relative L2), including a grid of exactly the array's
+512 x 512 cell limit.  They also check that the second call leaves device free
+memory unchanged and that problems just beyond the array's limits (cells,
+record channels, time steps) are refused with TOMO_ERR_ARG before any work.
 
 This file sorts last so that a run stopping at the first failure has already
 run every other test.
@@ -41,18 +43,26 @@ def phantom(seed, ny, nx):
     return f
 
 
-@pytest.mark.parametrize("make", [
-    lambda: tomo.cfg_config(nx=96, ny=80, nt=220, n_transducers=24, group_size=6, radius=30.0,
-                            cells_per_wavelength=10.0, sponge_width=10),
-    lambda: tomo.ref_config(nx=64, ny=60, nt=160, ring_lo=8, ring_hi=50, group_size=24),
-], ids=["cfg", "ref"])
-def test_noalloc_forward_matches_context_forward(built_lib, make):
+CASES = {
+    "cfg": lambda: tomo.cfg_config(nx=96, ny=80, nt=220, n_transducers=24, group_size=6, radius=30.0,
+                                   cells_per_wavelength=10.0, sponge_width=10),
+    "ref": lambda: tomo.ref_config(nx=64, ny=60, nt=160, ring_lo=8, ring_hi=50, group_size=24),
+    # exactly the array's cell limit (512 x 512), short run
+    "cfg-512": lambda: tomo.cfg_config(nx=512, ny=512, nt=90, n_transducers=32, group_size=8, radius=220.0),
+}
+
+
+@pytest.mark.parametrize("on_stream", [False, True], ids=["default-stream", "own-stream"])
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_noalloc_forward_matches_context_forward(built_lib, case, on_stream):
     import torch
 
-    cfg = make()
+    cfg = CASES[case]()
     dev = torch.device("cuda", 0)
     G, nch = tomo.n_groups(cfg), tomo.n_channels(cfg)
     d_rec = torch.empty((G, cfg.nt, nch), dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev) if on_stream else None
+    handle = C.c_void_p(stream.cuda_stream) if stream is not None else None
     with tomo.Context(cfg) as ctx:
         for call, seed in enumerate((1, 2)):
             f = phantom(seed, cfg.ny, cfg.nx)
@@ -61,8 +71,10 @@ def test_noalloc_forward_matches_context_forward(built_lib, make):
             torch.cuda.synchronize()
             free0 = torch.cuda.mem_get_info(dev)[0]
             st = built_lib.tomo_forward_noalloc(C.byref(cfg), C.c_void_p(d_f.data_ptr()),
-                                                C.c_void_p(d_rec.data_ptr()), None)
+                                                C.c_void_p(d_rec.data_ptr()), handle)
             assert st == tomo.OK
+            if stream is not None:
+                stream.synchronize()
             torch.cuda.synchronize()
             if call == 1:
                 # set-up was done by the first call; the second must not allocate
@@ -72,10 +84,18 @@ def test_noalloc_forward_matches_context_forward(built_lib, make):
             assert rel(got, want) <= TOL, (call, rel(got, want))
 
 
-def test_noalloc_rejects_oversized_problem(built_lib):
+@pytest.mark.parametrize("make,why", [
+    (lambda: tomo.cfg_config(nx=1024, ny=1024, nt=100, n_transducers=16, group_size=4, radius=400.0), "cells"),
+    # one row over 512 x 512
+    (lambda: tomo.cfg_config(nx=512, ny=513, nt=100, n_transducers=16, group_size=4, radius=200.0), "cells"),
+    # 4 * 516 = 2064 reference-profile channels, with fewer cells than the limit (516 x 508)
+    (lambda: tomo.ref_config(nx=516, ny=508, nt=100, ring_lo=20, ring_hi=480, group_size=40), "channels"),
+    (lambda: tomo.cfg_config(nx=64, ny=64, nt=16385, n_transducers=16, group_size=4, radius=20.0), "steps"),
+], ids=["1024x1024", "512x513", "ref-516x508", "nt-16385"])
+def test_noalloc_rejects_oversized_problem(built_lib, make, why):
     import torch
 
-    cfg = tomo.cfg_config(nx=1024, ny=1024, nt=100, n_transducers=16, group_size=4, radius=400.0)
+    cfg = make()
     d = torch.zeros(16, dtype=torch.float32, device="cuda")
     st = built_lib.tomo_forward_noalloc(C.byref(cfg), C.c_void_p(d.data_ptr()), C.c_void_p(d.data_ptr()), None)
-    assert st == tomo.ERR_ARG
+    assert st == tomo.ERR_ARG, why

@@ -12,24 +12,32 @@
 // that every GPU loading this library holds until the process exits.  It holds,
 // for one emitter group at a time, the three forward time slots, the two
 // coefficient fields and the geometry tables, so a call accepts grids of up to
-// kNoallocMaxCells cells (512 x 512), kNoallocMaxChannels record channels,
-// kNoallocMaxGroups groups, kNoallocMaxEmitters emitters and kNoallocMaxSteps
-// time steps, and rejects anything larger with TOMO_ERR_ARG.
+// kNoallocMaxCells cells (512 x 512), kNoallocMaxChannels record channels and
+// kNoallocMaxSteps time steps, plus kNoallocMaxEmitters emitters (benchmark
+// profile) or kNoallocMaxGroups emission boxes (reference profile), and rejects
+// anything larger with TOMO_ERR_ARG.
 //
-// In host code g_scratch names a host-side stand-in, not device memory; the
-// device address is looked up once per device with cudaGetSymbolAddress (the
-// first call on a device does it, with that device current -- make that first
-// call before any stream capture) and that pointer is what the kernels get.
+// In host code g_scratch names a host-side stand-in, not device memory.  Every
+// call looks the array's device address up with cudaGetSymbolAddress on the
+// current device and passes that pointer to the kernels, so the address is
+// right for whatever context is current (also after a cudaDeviceReset, which
+// reloads the module at a new address).  The first call on a device also loads
+// the module's code there: make that first call before any stream capture.
+//
+// The geometry tables travel to the array as kernel arguments (k_put_words),
+// not as copies from host memory, so nothing on the device side refers to the
+// call's host-side tables after it returns.
 //
 // All calls share the one array and it keeps the last call's contents: each
 // call zeroes the two initial time slots it starts from and the output records,
 // and rewrites everything else before reading it.  Calls that overlap on the
-// GPU (concurrent streams, or threads, on the same device) race on the array.
+// GPU (concurrent streams, or threads, on the same device) race on the array:
+// serialise them on one stream.
 #include <cuda_runtime.h>
 
 #include <cstdio>
 #include <cstring>
-#include <mutex>
+#include <algorithm>
 #include <string>
 
 #include "internal.h"
@@ -51,9 +59,17 @@ constexpr int64_t kNoallocScratchBytes = 4 * (kFloats + kInts);
 
 static __device__ __align__(256) unsigned char g_scratch[kNoallocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
+// Words of table data carried by one k_put_words launch (the argument block stays under the
+// 4 KB kernel-parameter limit of every CUDA version).
+constexpr int kWordsPerLaunch = 1000;
+struct Words {
+    uint32_t v[kWordsPerLaunch];
+};
+
+__global__ void k_put_words(uint32_t* __restrict__ dst, int n, Words w) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x) dst[t] = w.v[t];
+}
+
 // Failures are returned as a status and explained in one line on stderr.
 tomo_status fail(tomo_status s, const std::string& why) {
     std::fprintf(stderr, "tomo_forward_noalloc: %s\n", why.c_str());
@@ -64,20 +80,27 @@ tomo_status cuda_fail(cudaError_t e, const char* what) {
     return fail(TOMO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Device address of g_scratch on the current device (looked up once per device).
+// Device address of g_scratch in the current device's context, looked up on every call.
 tomo_status scratch_address(unsigned char** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-    if (dev < 0 || dev >= kMaxDevices) return fail(TOMO_ERR_ARG, "device ordinal too large");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || !p) return cuda_fail(e, "cudaGetSymbolAddress(g_scratch)");
-        g_addr[dev] = p;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess || !p) return cuda_fail(e, "cudaGetSymbolAddress(g_scratch)");
+    *out = (unsigned char*)p;
+    return TOMO_OK;
+}
+
+// Writes n 32-bit words from host memory to dst on `st`, kWordsPerLaunch per launch, through
+// kernel arguments: the words are captured at launch, so `src` may go out of scope on return.
+tomo_status put_words(uint32_t* dst, const void* src, int64_t n, cudaStream_t st) {
+    Words w;
+    const uint32_t* s = (const uint32_t*)src;
+    for (int64_t off = 0; off < n; off += kWordsPerLaunch) {
+        const int m = (int)std::min<int64_t>(kWordsPerLaunch, n - off);
+        std::memcpy(w.v, s + off, sizeof(uint32_t) * m);
+        k_put_words<<<1, 256, 0, st>>>(dst + off, m, w);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "k_put_words");
     }
-    *out = (unsigned char*)g_addr[dev];
     return TOMO_OK;
 }
 
@@ -94,10 +117,11 @@ extern "C" tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float*
     std::string why;
     tomo_status s = build_geometry(*cfg, geo, why);
     if (s != TOMO_OK) return fail(s, why);
-    if (geo.N > kNoallocMaxCells || geo.nch > kNoallocMaxChannels || geo.G > kNoallocMaxGroups ||
-        (int64_t)geo.G * geo.gs > kNoallocMaxEmitters || geo.nt > kNoallocMaxSteps)
+    // the emitter table is read by the benchmark profile only, the emission boxes by the reference profile
+    if (geo.N > kNoallocMaxCells || geo.nch > kNoallocMaxChannels || geo.nt > kNoallocMaxSteps ||
+        (geo.ref && geo.G > kNoallocMaxGroups) || (!geo.ref && (int64_t)geo.G * geo.gs > kNoallocMaxEmitters))
         return fail(TOMO_ERR_ARG, "problem exceeds the allocation-free limits (cells <= 262144, channels <= 2048, "
-                                  "groups <= 2048, emitters <= 4096, steps <= 16384)");
+                                  "steps <= 16384, emitters <= 4096, reference-profile groups <= 2048)");
     unsigned char* base = nullptr;
     if ((s = scratch_address(&base)) != TOMO_OK) return s;
     cudaStream_t st = (cudaStream_t)stream;
@@ -114,10 +138,11 @@ extern "C" tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float*
     do {                                             \
         if ((e = (x)) != cudaSuccess) return cuda_fail(e, #x); \
     } while (0)
-    NA_CU(cudaMemcpyAsync(src, geo.src.data(), sizeof(float) * nt, cudaMemcpyHostToDevice, st));
-    NA_CU(cudaMemcpyAsync(rcv, geo.rcv.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, st));
-    if (geo.ref) NA_CU(cudaMemcpyAsync(box, geo.box.data(), sizeof(int32_t) * 4 * geo.G, cudaMemcpyHostToDevice, st));
-    else NA_CU(cudaMemcpyAsync(emit, geo.emit.data(), sizeof(int32_t) * geo.G * geo.gs, cudaMemcpyHostToDevice, st));
+    if ((s = put_words((uint32_t*)src, geo.src.data(), nt, st)) != TOMO_OK) return s;
+    if ((s = put_words((uint32_t*)rcv, geo.rcv.data(), nch, st)) != TOMO_OK) return s;
+    if (geo.ref) s = put_words((uint32_t*)box, geo.box.data(), 4 * (int64_t)geo.G, st);
+    else s = put_words((uint32_t*)emit, geo.emit.data(), (int64_t)geo.G * geo.gs, st);
+    if (s != TOMO_OK) return s;
     NA_CU(cudaMemsetAsync(d_records, 0, sizeof(float) * (size_t)geo.G * nt * nch, st));
     DevGeo dg{};
     dg.nx = geo.nx; dg.ny = geo.ny; dg.nt = geo.nt; dg.nch = geo.nch;
