@@ -18,7 +18,7 @@ image error, with the speed-up, the gradient sweeps each used and the learned
 run's steps (L learned, x rejected proposal + plain step, p plain step).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl tomo|reference]
-                    [--workload c2|c1|c3|ref192|c5] [--no-cpu] [--no-learned]
+                    [--workload c2|c1|c3|ref192|c5] [--no-cpu] [--no-learned] [--nt T]
 Under torchrun each rank reconstructs its own independent phantom on its own
 GPU (weak scaling over independent reconstructions, no collective on the
 data path); rank 0 prints one JSON line.
@@ -360,10 +360,15 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the time-to-image leg (c2)")
+    ap.add_argument("--nt", type=int, default=0,
+                    help="time steps instead of the workload's (small cases for profiling; the workload "
+                         "name in the line says so)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     w = WORKLOADS.get(args.workload)
+    if w is not None and args.nt > 0 and w["cfg"] is not None:
+        w = dict(w, cfg=dict(w["cfg"], nt=args.nt), desc=w["desc"] + f" [nt {args.nt} instead]")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -219,6 +219,32 @@ tomo_status tomo_iterate_device(tomo_ctx* ctx, int32_t method, const tomo_schedu
                                 const float* d_f_true, tomo_iter_stats* stats);
 tomo_status tomo_synchronize(tomo_ctx* ctx);
 
+/* Group-sharded SIRT: the emitter groups of one iteration are independent, so
+ * they can be split over several contexts (one per GPU or process), which
+ * exchange their groups' correlations before the update.  The reference runs
+ * P of the M groups per pass on one GPU (sirt-mimo-norm-mem.cu:429-458); here
+ * a context runs the passes of its own group range and the caller moves the
+ * correlations between contexts (the reduce_df step).
+ *   tomo_gradient_groups_device  forward, residual, adjoint and correlation of
+ *       groups g0 .. g0+ng-1 for the field d_f (the context's records must be
+ *       set); their raw correlations C_g stay in the context, resid_norm2
+ *       (optional) receives their squared record residual;
+ *   tomo_get_correlations_device / tomo_set_correlations_device  copy the raw
+ *       correlations of groups g0 .. g0+ng-1 (ng*nx*ny floats, group-major)
+ *       out of / into the context, device to device on the context's stream;
+ *   tomo_update_device  the update rule of a SIRT method (every method but
+ *       TOMO_ART, which is sequential over groups) from the correlations the
+ *       context holds for all groups, applied to d_f; stats->resid_norm2 is NaN
+ *       (the caller sums the ranks' residuals).
+ * With every group's correlation in place, tomo_update_device gives the field
+ * tomo_iterate_device would, bit for bit. */
+tomo_status tomo_gradient_groups_device(tomo_ctx* ctx, const float* d_f, int32_t g0, int32_t ng,
+                                        double* resid_norm2);
+tomo_status tomo_get_correlations_device(tomo_ctx* ctx, int32_t g0, int32_t ng, float* d_out);
+tomo_status tomo_set_correlations_device(tomo_ctx* ctx, int32_t g0, int32_t ng, const float* d_in);
+tomo_status tomo_update_device(tomo_ctx* ctx, int32_t method, const tomo_schedule* sched, int32_t iter,
+                               float* d_f, const float* d_f_true, tomo_iter_stats* stats);
+
 /* Profiling hook (no reference counterpart): runs `steps` consecutive time steps
  * of one hot kernel for the first pass's groups on the context stream, bracketed
  * by CUDA events, after at least one tomo_iterate.  which: 0 forward step,

@@ -323,7 +323,6 @@ void adjoint_ref(const Problem& P, const Coef<T>& K, const T* u, const T* rr, do
     const T* of = K.onef.data();
     const T A = T(1500) * T(1500) * (T(RDT) * T(RDT));
     const T HH = T(RH) * T(RH);
-    const T inj = T(RH) * T(1000);
 #pragma omp parallel num_threads(nth)
     for (int k = nt - 2; k > 0; --k) {
         T* zk = zb.data() + (size_t)(k % 3) * N;
@@ -342,12 +341,13 @@ void adjoint_ref(const Problem& P, const Coef<T>& K, const T* u, const T* rr, do
             }
 #pragma omp single
         {
-            // backpropagation2 (sirt-mimo.cu:712-774): sensor lines, then edges, then corners.
+            // backpropagation2 (sirt-mimo.cu:712-774): sensor lines (z + (rr H) 1000, the
+            // reference's order), then edges, then corners.
             for (int i = lo + 1; i < hi; ++i) {
-                zk[hi * nx + i] = zk[(hi - 1) * nx + i] + rk[0 * nx + i] * inj;
-                zk[lo * nx + i] = zk[(lo + 1) * nx + i] + rk[2 * nx + i] * inj;
-                zk[i * nx + hi] = zk[i * nx + hi - 1] + rk[1 * nx + i] * inj;
-                zk[i * nx + lo] = zk[i * nx + lo + 1] + rk[3 * nx + i] * inj;
+                zk[hi * nx + i] = zk[(hi - 1) * nx + i] + rk[0 * nx + i] * T(RH) * T(1000);
+                zk[lo * nx + i] = zk[(lo + 1) * nx + i] + rk[2 * nx + i] * T(RH) * T(1000);
+                zk[i * nx + hi] = zk[i * nx + hi - 1] + rk[1 * nx + i] * T(RH) * T(1000);
+                zk[i * nx + lo] = zk[i * nx + lo + 1] + rk[3 * nx + i] * T(RH) * T(1000);
             }
             for (int i = 1; i < nx - 1; ++i) {
                 zk[i] = zk[nx + i];
@@ -662,6 +662,34 @@ int orc_gradient(const tomo_config* cfg, int prec, int threads, const double* f,
     const int nth = nthreads(threads);
     if (prec == 32) gradient_all<float>(P, f, meas, dfg, resid2, nth);
     else gradient_all<double>(P, f, meas, dfg, resid2, nth);
+    return TOMO_OK;
+}
+
+int orc_gradient_groups(const tomo_config* cfg, int prec, int threads, const double* f, const float* meas, int g0,
+                        int ng, double* dfg, double* resid2) {
+    Problem P;
+    const int st = setup(cfg, P);
+    if (st) return st;
+    if (!f || !meas || g0 < 0 || ng < 1 || g0 + ng > P.G) return TOMO_ERR_ARG;
+    const int nth = nthreads(threads);
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        Coef<T> K;
+        make_coef<T>(P, f, K);
+        std::vector<T> hist((size_t)P.nt * P.N);
+        std::vector<double> corr(P.N);
+        double r2 = 0.0;
+        for (int g = g0; g < g0 + ng; ++g) {
+            std::fill(corr.begin(), corr.end(), 0.0);
+            group_sweep<T>(P, K, g, hist, meas, nullptr, corr.data(), &r2, nth);
+            if (dfg)
+                for (int q = 0; q < P.N; ++q)
+                    dfg[(size_t)(g - g0) * P.N + q] = corr[q] * P.corr_scale / (1.0 + f[q]);
+        }
+        if (resid2) *resid2 = r2;
+    };
+    if (prec == 32) run(float{});
+    else run(double{});
     return TOMO_OK;
 }
 

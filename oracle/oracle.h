@@ -48,6 +48,11 @@ int orc_forward(const tomo_config* cfg, int prec, int threads, const double* f,
 int orc_gradient(const tomo_config* cfg, int prec, int threads, const double* f,
                  const float* meas, double* dfg, double* resid2);
 
+/* The same for groups g0 .. g0+ng-1 only: dfg (ng*nx*ny, optional) and their
+ * squared record residual (optional). */
+int orc_gradient_groups(const tomo_config* cfg, int prec, int threads, const double* f,
+                        const float* meas, int g0, int ng, double* dfg, double* resid2);
+
 /* One iteration of `method`; stats[0]=epsilon (NaN without f_true),
  * stats[1]=resid2 at the start, stats[2]=scale. */
 int orc_iterate(const tomo_config* cfg, int prec, int threads, int method,

@@ -52,10 +52,11 @@ def lib() -> C.CDLL:
         L.orc_phantom_ref.argtypes = [i32, i32, FP]
         L.orc_forward.argtypes = [CP, i32, i32, DP, FP, DP]
         L.orc_gradient.argtypes = [CP, i32, i32, DP, FP, DP, DP]
+        L.orc_gradient_groups.argtypes = [CP, i32, i32, DP, FP, i32, i32, DP, DP]
         L.orc_iterate.argtypes = [CP, i32, i32, i32, C.POINTER(tomo.Schedule), i32, DP, FP, DP, DP]
         L.orc_sweep.argtypes = [CP, i32, i32, DP, FP, i32, i32, DP]
         for n in ("orc_info_get", "orc_transducers", "orc_mask", "orc_phantom_ref", "orc_forward",
-                  "orc_gradient", "orc_iterate", "orc_sweep"):
+                  "orc_gradient", "orc_gradient_groups", "orc_iterate", "orc_sweep"):
             getattr(L, n).restype = i32
         _L = L
     return _L
@@ -117,6 +118,17 @@ def gradient(cfg, f, meas, prec=64, threads=0):
     dfg = np.zeros((inf["n_groups"], cfg.ny, cfg.nx), np.float64)
     r2 = C.c_double()
     _chk(lib().orc_gradient(C.byref(cfg), prec, threads, _d(f), _f(meas), _d(dfg), C.byref(r2)), "gradient")
+    return dfg, r2.value
+
+
+def gradient_groups(cfg, f, meas, g0, ng, prec=64, threads=0):
+    """Per-group gradients of groups g0 .. g0+ng-1 only (ng, ny, nx) and their squared residual."""
+    f = np.ascontiguousarray(f, np.float64)
+    meas = np.ascontiguousarray(meas, np.float32)
+    dfg = np.zeros((ng, cfg.ny, cfg.nx), np.float64)
+    r2 = C.c_double()
+    _chk(lib().orc_gradient_groups(C.byref(cfg), prec, threads, _d(f), _f(meas), g0, ng, _d(dfg), C.byref(r2)),
+         "gradient_groups")
     return dfg, r2.value
 
 

@@ -1,12 +1,16 @@
 """GPU checks of the command-line drivers built on the C ABI: the hybrid ART -> SIRT driver
 (sirt-mimo-seq.cu) and the alternating-relaxation driver (sirt-mimo-norm-alt.cu) give the
-same epsilons and image as the same method/schedule sequence through tomo_iterate."""
+same epsilons and image as the same method/schedule sequence through tomo_iterate, and the
+FP64 oracle replaying that sequence on the same records gives the same epsilons and image
+within the reference-profile parity bars (1e-4 relative, widened to three times the
+reference scheme's own FP32-vs-FP64 distance where that is larger)."""
 import os
 import subprocess
 
 import numpy as np
 import pytest
 
+import oracle_lib as O
 import tomo
 
 pytestmark = pytest.mark.gpu
@@ -48,6 +52,39 @@ def api_run(methods, scales, gs=160):
     return eps, f
 
 
+def oracle_replay(methods, scales, rec, fo, prec, gs=160):
+    """The oracle's epsilons and image for the same sequence and stopping rule."""
+    cfg = tomo.ref_config(group_size=gs)
+    f = np.zeros(fo.shape, np.float64)
+    eps, prev = [], 100.0
+    for it, (m, sc) in enumerate(zip(methods, scales)):
+        e = O.iterate(cfg, m, sc, it, f, rec, fo.astype(np.float64), prec=prec)[0]
+        eps.append(e)
+        if e > prev:
+            break
+        prev = e
+    return eps, f
+
+
+def check_against_oracle(eps_cli, img_cli, methods, scales, tmp):
+    """eps_cli and the driver's image against the oracle on the driver's own records."""
+    fo = tomo.phantom_ref()
+    with tomo.Context(tomo.ref_config(group_size=160)) as ctx:
+        rec = ctx.generate_data(fo)            # the records generate-data wrote, bit for bit
+    eps64, f64 = oracle_replay(methods, scales, rec, fo, 64)
+    eps32, f32 = oracle_replay(methods, scales, rec, fo, 32)
+    n = min(len(eps_cli), len(eps64), len(eps32))
+    assert n >= 5
+    for it in range(n):
+        tol = max(1e-4 * eps64[it], 3 * abs(eps32[it] - eps64[it]))
+        assert abs(eps_cli[it] - eps64[it]) <= tol, (it, eps_cli[it], eps64[it], tol)
+    if len(eps_cli) == len(eps64) == len(eps32):
+        tol = max(1e-4, 3 * (np.linalg.norm(f32 - f64) / np.linalg.norm(f64)))
+        err = np.linalg.norm(img_cli - f64) / np.linalg.norm(f64)
+        assert err <= tol, (f"image vs oracle {err:.2e} (bar {tol:.2e}); image error vs phantom "
+                            f"{100 * np.linalg.norm(img_cli - fo) / np.linalg.norm(fo):.3f} %")
+
+
 def prepare(tmp):
     run(tmp, "generate-field")
     run(tmp, "generate-data", "fo.txt", "160")
@@ -64,20 +101,23 @@ def test_cli_hybrid_art_then_sirt(built_lib, tmp_path):
     img = np.array(open(tmp_path / "sirt-norm-160-fo.txt").read().split(), np.float32).reshape(192, 192)
     if len(eps_api) == 7:
         assert np.array_equal(img, f_api)
+    check_against_oracle(eps_cli, img, [tomo.ART] * 5 + [tomo.SIRT_NORM] * 2, [sched] * 7, tmp_path)
 
 
 def test_cli_alternating_relaxation(built_lib, tmp_path):
     prepare(tmp_path)
-    out = run(tmp_path, "sirt-mimo-norm-alt", "fo.txt", "160", "0", "0", "6", "100", "20", "1", "60", "10", "1")
+    out = run(tmp_path, "sirt-mimo-norm-alt", "fo.txt", "160", "0", "0", "6", "10", "2", "1", "6", "1", "1")
     eps_cli = table_eps(out)
     scales = []
     for it in range(6):
         k = it + 1
-        s = 1e5 + 2e4 / k if k % 2 else 6e4 - 1e4 / k
+        s = 1e4 + 2e3 / k if k % 2 else 6e3 - 1e3 / k
         scales.append(tomo.schedule(tomo.SCHED_CONST, np.float32(s)))
     eps_api, f_api = api_run([tomo.SIRT_NORM] * 6, scales)
     assert len(eps_cli) == len(eps_api) and np.all(np.isfinite(eps_api))
     assert np.allclose(eps_cli, eps_api, rtol=1e-6, atol=0)
+    img = np.array(open(tmp_path / "sirt-norm-160-fo.txt").read().split(), np.float32).reshape(192, 192)
+    check_against_oracle(eps_cli, img, [tomo.SIRT_NORM] * 6, scales, tmp_path)
 
 
 def test_cli_binary_files_match_text(built_lib, tmp_path):

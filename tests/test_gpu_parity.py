@@ -4,11 +4,16 @@ Tolerances (relative L2, stated by the project's correctness target):
   wavefield / records after nt steps   <= 1e-5
   per-group gradients                  <= 1e-4
   reconstructed images                 <= 1e-4
-For the reference profile each bound is widened to three times the distance
-of the reference scheme's own FP32 arithmetic (the oracle's prec=32 mode)
-from FP64 when that distance is larger: the reference's one-way absorbing
-edges amplify rounding, so its FP32 results sit 1e-5..1e-4 from FP64 and its
-gradients, through the residual's cancellation, up to ~1e-3.
+For the reference profile each bound against FP64 is widened to three times
+the distance of the reference scheme's own FP32 arithmetic (the oracle's
+prec=32 mode) from FP64 when that distance is larger: the reference's one-way
+absorbing edges amplify rounding, so its FP32 results sit 1e-5..1e-4 from
+FP64 and its gradients, through the residual's cancellation, up to ~1e-3.
+Against the oracle's FP32 transcription itself the reference profile meets
+the unwidened bars: its kernels evaluate the reference's formulas in the
+reference's operation order with every operation rounded, so wavefields and
+records are equal bit for bit and gradients and images agree within 1e-4
+(the correlation sums in FP32 here and in FP64 in the oracle).
 Checkpoint/recompute and multi-pass schedules must reproduce the
 single-pass full-history result exactly (same kernels, same operands).
 """
@@ -83,6 +88,25 @@ def test_forward_records_and_wavefield(maker):
     tol_u, tol_r = field_tol(cfg, fo, ul_o, rec_o)
     assert rel(ul, ul_o) <= tol_u
     assert rel(rec, rec_o) <= tol_r
+
+
+@pytest.mark.parametrize("maker,kw", [(None, {}), ("ragged", dict(nx=63, ny=57, ring_lo=8, ring_hi=48, group_size=20)),
+                                      ("full", {})], ids=["64x60", "63x57", "192x192"])
+def test_ref_profile_matches_fp32_transcription(maker, kw):
+    """Reference profile against the oracle's FP32 transcription at the unwidened bars: records
+    and last wavefields bit for bit, per-group gradients and their residual within 1e-4."""
+    cfg = tomo.ref_config(group_size=160) if maker == "full" else small_ref(**kw)
+    fo = tomo.phantom_ref() if maker == "full" else blob_phantom(cfg.ny, cfg.nx, seed=21)
+    f = blob_phantom(cfg.ny, cfg.nx, seed=22, amp=0.01)
+    rec32, ul32 = O.forward(cfg, fo.astype(np.float64), prec=32, u_last=True)
+    with tomo.Context(cfg) as ctx:
+        rec, ul = ctx.forward(fo, u_last=True)
+        assert np.array_equal(rec, rec32), rel(rec, rec32)
+        assert np.array_equal(ul.astype(np.float64), ul32), rel(ul, ul32)
+        dfg, _, r2 = ctx.gradient(f, rec32)
+    dfg32, r2_32 = O.gradient(cfg, f.astype(np.float64), rec32, prec=32)
+    assert rel(dfg, dfg32) <= TOL_GRAD, rel(dfg, dfg32)
+    assert abs(r2 - r2_32) <= 1e-6 * r2_32
 
 
 def test_forward_reference_problem_full_size():
@@ -170,6 +194,9 @@ def test_methods_ref_three_iterations(method, sched):
                 assert abs(st.resid_norm2 - r2_at) <= max(1e-4 * r2_at, 3 * abs(r2_at32 - r2_at))
             assert rel(f, f_o) <= tol, (it, rel(f, f_o), tol)
             assert abs(st.epsilon - eps_o) <= max(1e-4 * eps_o, 3 * abs(eps_32 - eps_o))
+            # and against the reference scheme's FP32 transcription at the unwidened bars
+            assert rel(f, f_32) <= TOL_IMG, (it, rel(f, f_32))
+            assert abs(st.epsilon - eps_32) <= 1e-4 * eps_32, (it, st.epsilon, eps_32)
 
 
 @pytest.mark.parametrize("method", [tomo.SIRT_CLASSIC, tomo.SIRT_NORM, tomo.ART])

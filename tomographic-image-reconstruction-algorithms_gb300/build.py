@@ -63,8 +63,11 @@ def _run(cmd: list[str]) -> None:
 def _compile(src: str, obj: str) -> None:
     cmd = [NVCC, *ARCH, *COMMON, "-Xcompiler", "-fPIC", "-c", src, "-o", obj]
     if src.endswith(".cpp"):
+        # host arithmetic (the reference-profile source table) rounds every operation, as the
+        # oracle does: no fused multiply-add contraction on either host architecture
         cmd.insert(1, "-x")
         cmd.insert(2, "c++")
+        cmd += ["-Xcompiler", "-ffp-contract=off"]
     _run(cmd)
 
 

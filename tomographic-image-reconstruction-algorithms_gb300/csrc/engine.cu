@@ -157,7 +157,7 @@ void fwd_launch(tomo_ctx* c, const FwdStep& fs) {
 
 void adj_launch(tomo_ctx* c, const AdjStep& as) {
     if (c->strip) launch_adj_strip(c->rows_adj, c->adj_variant, c->dg, c->coef, as, c->st);
-    else launch_adj_step(c->geo.cfg.profile, c->dg, c->coef, as, c->st);
+    else launch_adj_step(c->geo.cfg.profile, c->dg, c->coef, c->f, as, c->st);
 }
 
 FwdStep fwd_args(tomo_ctx* c, int k, int g0, int ng) {
@@ -413,7 +413,7 @@ tomo_status create_buffers(tomo_ctx* c) {
     TRY(c->alloc(&c->sums, G + 8, "sums"));
     TRY(c->alloc(&c->maxabs, 1, "maxabs"));
     TRY(c->alloc(&c->mask, N, "mask"));
-    TRY(c->alloc(&c->src, nt, "source"));
+    TRY(c->alloc(&c->src, (int64_t)g.src.size(), "source"));
     TRY(c->alloc(&c->rcv, nch, "receivers"));
     if (g.ref) TRY(c->alloc(&c->box, 4 * G, "boxes"));
     else {
@@ -427,7 +427,7 @@ tomo_status create_buffers(tomo_ctx* c) {
     CU(c, cudaMemsetAsync(c->rpart, 0, sizeof(double) * G * nt, c->st));
     CU(c, cudaMemsetAsync(c->f, 0, sizeof(float) * N, c->st));
     CU(c, cudaMemcpyAsync(c->mask, g.mask.data(), N, cudaMemcpyHostToDevice, c->st));
-    CU(c, cudaMemcpyAsync(c->src, g.src.data(), sizeof(float) * nt, cudaMemcpyHostToDevice, c->st));
+    CU(c, cudaMemcpyAsync(c->src, g.src.data(), sizeof(float) * g.src.size(), cudaMemcpyHostToDevice, c->st));
     CU(c, cudaMemcpyAsync(c->rcv, g.rcv.data(), sizeof(int32_t) * nch, cudaMemcpyHostToDevice, c->st));
     if (g.ref) CU(c, cudaMemcpyAsync(c->box, g.box.data(), sizeof(int32_t) * 4 * G, cudaMemcpyHostToDevice, c->st));
     else {
@@ -721,6 +721,77 @@ tomo_status epsilon(tomo_ctx* c, double* out) {
     return TOMO_OK;
 }
 
+// The update rule of a SIRT method from the correlations of all groups held in c->corr, applied
+// to c->f (every method but ART, which updates after each group).
+tomo_status update_core(tomo_ctx* c, int method, const tomo_schedule* sch, double s) {
+    const Geometry& g = c->geo;
+    const int64_t N = g.N;
+    const int G = g.G;
+    const double sc = g.corr_scale;
+    const int nb = reduce_blocks();
+    switch (method) {
+    case TOMO_SIRT_CLASSIC:
+        launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0, c->dir, c->st);
+        ++c->launches;
+        TRY(apply_dir(c, sch, s));
+        break;
+    case TOMO_SIRT_SCALED:
+    case TOMO_SIRT_WEIGHT:
+    case TOMO_SIRT_AVG:
+        launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->dir, c->st);
+        ++c->launches;
+        TRY(apply_dir(c, sch, s));
+        break;
+    case TOMO_SIRT_NORM: {
+        // mean, per-group deviation norms, inverse-norm weights (sirt-mimo-norm.cu:56-118)
+        launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->tmp, c->st);
+        launch_group_dev_norm(c->corr, G, N, c->f, sc, c->tmp, c->part, nb, c->st);
+        launch_sum_parts(c->part, G, nb, c->sums, c->st);
+        c->launches += 3;
+        std::vector<double> d2(G);
+        CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
+        CU(c, cudaStreamSynchronize(c->st));
+        std::vector<double> w(G);
+        double W = 0.0;
+        for (int gg = 0; gg < G; ++gg) { w[gg] = 1.0 / std::sqrt(d2[gg]); W += w[gg]; }
+        for (int gg = 0; gg < G; ++gg) w[gg] /= W;
+        CU(c, cudaMemcpyAsync(c->sums, w.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
+        launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
+        ++c->launches;
+        TRY(apply_dir(c, sch, s));
+        CU(c, cudaStreamSynchronize(c->st));   // w lives on the host stack
+        break;
+    }
+    case TOMO_SIRT_AVG_WEIGHT: {
+        // fg = f + s*mask*df_g; f += sum_g fg/||fg - mean fg|| (sirt-mimo-avg-weight.cu:130-203)
+        launch_avgw_fbar(c->corr, G, N, c->f, c->mask, sc, s, c->tmp, c->st);
+        launch_avgw_norm(c->corr, G, N, c->f, c->mask, sc, s, c->tmp, c->part, nb, c->st);
+        launch_sum_parts(c->part, G, nb, c->sums, c->st);
+        launch_avgw_apply(c->corr, G, N, c->f, c->mask, sc, s, c->sums, c->st);
+        c->launches += 4;
+        break;
+    }
+    default:
+        return c->fail(TOMO_ERR_ARG, "method %d has no update from held correlations", method);
+    }
+    return TOMO_OK;
+}
+
+// Fills the iteration statistics from the events ev0/ev1 around the iteration's device work.
+void fill_stats(tomo_ctx* c, tomo_iter_stats* stats, double eps, double r2, double s, double groups,
+                int64_t launches0) {
+    if (!stats) return;
+    const Geometry& g = c->geo;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    stats->epsilon = eps;
+    stats->resid_norm2 = r2;
+    stats->scale = s;
+    stats->seconds = ms * 1e-3;
+    stats->cell_updates = 2.0 * groups * (double)(g.nt - 2) * (double)g.N;
+    stats->kernel_launches = (double)(c->launches - launches0);
+}
+
 // One iteration on c->f with c->meas; f_true in c->ftrue when have_true.
 tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int it, bool have_true,
                          tomo_iter_stats* stats) {
@@ -732,7 +803,6 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
     const double s = sched_scale(sch, it);
     if (!std::isfinite(s)) return c->fail(TOMO_ERR_ARG, "bad schedule");
     const double sc = g.corr_scale;
-    const int nb = reduce_blocks();
     const int64_t launches0 = c->launches;
     CU(c, cudaEventRecord(c->ev0, c->st));
     double r2 = 0.0;
@@ -753,67 +823,14 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
     } else {
         TRY(gradient_all(c));
         TRY(residual_norm(c, &r2));
-        switch (method) {
-        case TOMO_SIRT_CLASSIC:
-            launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0, c->dir, c->st);
-            ++c->launches;
-            TRY(apply_dir(c, sch, s));
-            break;
-        case TOMO_SIRT_SCALED:
-        case TOMO_SIRT_WEIGHT:
-        case TOMO_SIRT_AVG:
-            launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->dir, c->st);
-            ++c->launches;
-            TRY(apply_dir(c, sch, s));
-            break;
-        case TOMO_SIRT_NORM: {
-            // mean, per-group deviation norms, inverse-norm weights (sirt-mimo-norm.cu:56-118)
-            launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->tmp, c->st);
-            launch_group_dev_norm(c->corr, G, N, c->f, sc, c->tmp, c->part, nb, c->st);
-            launch_sum_parts(c->part, G, nb, c->sums, c->st);
-            c->launches += 3;
-            std::vector<double> d2(G);
-            CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
-            CU(c, cudaStreamSynchronize(c->st));
-            std::vector<double> w(G);
-            double W = 0.0;
-            for (int gg = 0; gg < G; ++gg) { w[gg] = 1.0 / std::sqrt(d2[gg]); W += w[gg]; }
-            for (int gg = 0; gg < G; ++gg) w[gg] /= W;
-            CU(c, cudaMemcpyAsync(c->sums, w.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
-            launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
-            ++c->launches;
-            TRY(apply_dir(c, sch, s));
-            CU(c, cudaStreamSynchronize(c->st));   // w lives on the host stack
-            break;
-        }
-        case TOMO_SIRT_AVG_WEIGHT: {
-            // fg = f + s*mask*df_g; f += sum_g fg/||fg - mean fg|| (sirt-mimo-avg-weight.cu:130-203)
-            launch_avgw_fbar(c->corr, G, N, c->f, c->mask, sc, s, c->tmp, c->st);
-            launch_avgw_norm(c->corr, G, N, c->f, c->mask, sc, s, c->tmp, c->part, nb, c->st);
-            launch_sum_parts(c->part, G, nb, c->sums, c->st);
-            launch_avgw_apply(c->corr, G, N, c->f, c->mask, sc, s, c->sums, c->st);
-            c->launches += 4;
-            break;
-        }
-        default:
-            return c->fail(TOMO_ERR_ARG, "unknown method %d", method);
-        }
+        TRY(update_core(c, method, sch, s));
     }
     CU(c, cudaEventRecord(c->ev1, c->st));
     double eps = std::numeric_limits<double>::quiet_NaN();
     if (have_true) TRY(epsilon(c, &eps));
     CU(c, cudaStreamSynchronize(c->st));
     CU(c, cudaGetLastError());
-    if (stats) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-        stats->epsilon = eps;
-        stats->resid_norm2 = r2;
-        stats->scale = s;
-        stats->seconds = ms * 1e-3;
-        stats->cell_updates = 2.0 * (double)G * (double)(g.nt - 2) * (double)N;
-        stats->kernel_launches = (double)(c->launches - launches0);
-    }
+    fill_stats(c, stats, eps, r2, s, (double)G, launches0);
     return TOMO_OK;
 }
 
@@ -1163,6 +1180,80 @@ tomo_status tomo_iterate_device(tomo_ctx* c, int32_t method, const tomo_schedule
     if (d_f_true) CU(c, cudaMemcpyAsync(c->ftrue, d_f_true, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
     TRY(iterate_core(c, method, sched, iter, d_f_true != nullptr, stats));
     CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
+}
+
+tomo_status tomo_gradient_groups_device(tomo_ctx* c, const float* d_f, int32_t g0, int32_t ng,
+                                       double* resid_norm2) try {
+    if (!c || !d_f) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    const Geometry& g = c->geo;
+    if (g0 < 0 || ng < 1 || g0 > g.G - ng) return c->fail(TOMO_ERR_ARG, "group range %d + %d outside 0..%d", g0, ng, g.G);
+    if (!c->meas_set) return c->fail(TOMO_ERR_STATE, "no measured records");
+    CU(c, cudaSetDevice(c->dev));
+    CU(c, cudaMemcpyAsync(c->f, d_f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    TRY(next_noise_draw(c));
+    launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
+    ++c->launches;
+    for (int a = g0; a < g0 + ng; a += c->P) TRY(run_pass(c, MODE_GRAD, a, std::min(c->P, g0 + ng - a)));
+    if (resid_norm2) {
+        launch_sum_parts(c->rpart + (int64_t)g0 * g.nt, 1, ng * g.nt, c->sums, c->st);
+        ++c->launches;
+        CU(c, cudaMemcpyAsync(resid_norm2, c->sums, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    }
+    CU(c, cudaStreamSynchronize(c->st));
+    CU(c, cudaGetLastError());
+    return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
+}
+
+tomo_status tomo_get_correlations_device(tomo_ctx* c, int32_t g0, int32_t ng, float* d_out) try {
+    if (!c || !d_out) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    const Geometry& g = c->geo;
+    if (g0 < 0 || ng < 1 || g0 > g.G - ng) return c->fail(TOMO_ERR_ARG, "group range %d + %d outside 0..%d", g0, ng, g.G);
+    CU(c, cudaSetDevice(c->dev));
+    CU(c, cudaMemcpyAsync(d_out, c->corr + (int64_t)g0 * g.N, sizeof(float) * (size_t)ng * g.N,
+                          cudaMemcpyDeviceToDevice, c->st));
+    return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
+}
+
+tomo_status tomo_set_correlations_device(tomo_ctx* c, int32_t g0, int32_t ng, const float* d_in) try {
+    if (!c || !d_in) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    const Geometry& g = c->geo;
+    if (g0 < 0 || ng < 1 || g0 > g.G - ng) return c->fail(TOMO_ERR_ARG, "group range %d + %d outside 0..%d", g0, ng, g.G);
+    CU(c, cudaSetDevice(c->dev));
+    CU(c, cudaMemcpyAsync(c->corr + (int64_t)g0 * g.N, d_in, sizeof(float) * (size_t)ng * g.N,
+                          cudaMemcpyDeviceToDevice, c->st));
+    return TOMO_OK;
+} catch (...) {
+    return abi_exception(c ? &c->err : nullptr);
+}
+
+tomo_status tomo_update_device(tomo_ctx* c, int32_t method, const tomo_schedule* sched, int32_t iter, float* d_f,
+                               const float* d_f_true, tomo_iter_stats* stats) try {
+    if (!c || !d_f || !sched) return c ? c->fail(TOMO_ERR_ARG, "NULL argument") : TOMO_ERR_ARG;
+    if (method < 0 || method >= TOMO_METHOD_COUNT || method == TOMO_ART)
+        return c->fail(TOMO_ERR_ARG, "tomo_update_device takes a SIRT method (not ART), got %d", method);
+    const double s = sched_scale(sched, iter);
+    if (!std::isfinite(s)) return c->fail(TOMO_ERR_ARG, "bad schedule");
+    CU(c, cudaSetDevice(c->dev));
+    const Geometry& g = c->geo;
+    const int64_t launches0 = c->launches;
+    CU(c, cudaMemcpyAsync(c->f, d_f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    if (d_f_true) CU(c, cudaMemcpyAsync(c->ftrue, d_f_true, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    CU(c, cudaEventRecord(c->ev0, c->st));
+    TRY(update_core(c, method, sched, s));
+    CU(c, cudaEventRecord(c->ev1, c->st));
+    double eps = std::numeric_limits<double>::quiet_NaN();
+    if (d_f_true) TRY(epsilon(c, &eps));
+    CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    CU(c, cudaGetLastError());
+    fill_stats(c, stats, eps, std::numeric_limits<double>::quiet_NaN(), s, 0.0, launches0);
     return TOMO_OK;
 } catch (...) {
     return abi_exception(c ? &c->err : nullptr);

@@ -67,14 +67,17 @@ tomo_status build_geometry(const tomo_config& c, Geometry& geo, std::string& why
         geo.mask.assign(geo.N, 0);
         for (int j = geo.lo + 1; j < geo.hi; ++j)
             std::memset(geo.mask.data() + (int64_t)j * nx + geo.lo + 1, 1, geo.hi - geo.lo - 1);
-        // Source factor per step: h^2 * wavelet(k); the kernel multiplies by r^2,
-        // giving v^2 dt^2 * wavelet.  Emitted while k + 1 <= 24.
+        // Source (sirt-mimo.cu:553-561), emitted while k + 1 <= 24: the kernel forms
+        // v v DT DT cos(wc t) exp(-t^2 / 2 tau^2) per cell in FP32, in that order; the two
+        // transcendental factors are evaluated here in FP32 (t = k DT - TT) and tabled as
+        // src[k] = cos(wc t) and src[n + k] = exp(-t^2 / 2 tau^2), n = n_src_steps.
         geo.n_src_steps = std::min(24, c.nt - 1);
-        geo.src.assign(c.nt, 0.f);
-        const double h = kRefH, wc = kRefOmegaC, tau = kRefTao;
-        for (int k = 0; k < geo.n_src_steps; ++k) {
-            const double t = (double)((float)k * kRefDT - kRefTT);   // float t as sirt-mimo.cu:555
-            geo.src[k] = (float)(h * h * std::cos(wc * t) * std::exp(-(t * t) / (2.0 * tau * tau)));
+        const int n = geo.n_src_steps;
+        geo.src.assign(std::max(c.nt, 2 * n), 0.f);
+        for (int k = 0; k < n; ++k) {
+            const float t = (float)k * kRefDT - kRefTT;
+            geo.src[k] = std::cos(kRefOmegaC * t);
+            geo.src[n + k] = std::exp(-(t * t) / (2.f * kRefTao * kRefTao));
         }
         const float hh = kRefH * kRefH;
         geo.corr_scale = 1.0 / (double)hh;

@@ -88,7 +88,8 @@ struct Geometry {
     std::vector<int32_t> rcv;          // receiver cell per channel, -1 none
     std::vector<int32_t> rid;          // CFG: per-cell channel index or -1
     std::vector<uint8_t> mask;         // update mask
-    std::vector<float> src;            // per step source factor (REF: h^2 * wavelet(k); CFG: C^2 ricker(n))
+    std::vector<float> src;            // CFG: per step C^2 ricker(n); REF: the FP32 factors cos(wc t_k) at
+                                       // [k] and exp(-t_k^2 / 2 tau^2) at [n_src_steps + k]
     int n_src_steps = 0;               // steps k (computing u(k+1)) that add a source
     double corr_scale = 1.0;           // REF 1/h^2, CFG C^2
 };
@@ -131,7 +132,7 @@ struct DevGeo {
     const int32_t* rid;    // CFG per-cell channel or -1
     const uint32_t* rbits; // CFG per row: bit b set when cells [32b, 32b+32) hold a receiver
     int rwords;            // words of rbits per row
-    const float* src;      // per step source factor
+    const float* src;      // source table (Geometry::src)
     int n_src_steps;
     // residual noise: simulated samples u become u * noise_factor(*noise_key, noise_level, ...)
     // in every residual gather while noise_key is non-null (its value can change between passes)
@@ -186,7 +187,9 @@ void launch_coef(int profile, const float* f, float* coef, float* rcoef, int64_t
                  void* stream);
 void launch_fwd_step(int profile, const DevGeo& g, const float* coef, const float* rcoef,
                      const FwdStep& s, void* stream);
-void launch_adj_step(int profile, const DevGeo& g, const float* coef, const AdjStep& s, void* stream);
+// f: the field the coefficients were made from (the reference-profile adjoint reads 1 + f)
+void launch_adj_step(int profile, const DevGeo& g, const float* coef, const float* f, const AdjStep& s,
+                     void* stream);
 void launch_gather(const DevGeo& g, const GatherStep& s, void* stream);
 void launch_fill(float* p, int64_t n, float v, void* stream);
 // zero slots off0 and off1 (element offsets) of ng groups spaced gstride apart

@@ -30,26 +30,34 @@ constexpr int RED_THREADS = 256;
 __device__ __forceinline__ float ldg(const float* p) { return __ldg(p); }
 
 // ---------------------------------------------------------------------------
-// Coefficients of one field: REF c = r^2 with r = 1500 sqrt(1+f) dt/h
-// (sirt-mimo.cu:525-526), rc = r; CFG c = C^2 (1+f).  Evaluated in FP64 and
-// rounded once.
+// Explicitly rounded FP32 operations: the reference-profile kernels evaluate the reference's
+// formulas in its operation order with every operation rounded to nearest and nothing
+// contracted into a fused multiply-add, so they give the bits of the oracle's FP32 transcription
+// of the reference (compiled without contraction) on every GPU and host.
+__device__ __forceinline__ float rm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float ra(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rs(float a, float b) { return __fsub_rn(a, b); }
+
+// Coefficients of one field.  REF (sirt-mimo.cu:525-526): v = 1500 sqrt(1+f),
+// r = v dt / h in FP32, coef = r*r, rcoef = v (r is recomputed from v where needed, with the
+// same operations).  CFG: c = C^2 (1+f) evaluated in FP64 and rounded once.
 __global__ void k_coef(int profile, const float* __restrict__ f, float* __restrict__ coef,
                        float* __restrict__ rcoef, int64_t N, float courant) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < N; q += (int64_t)gridDim.x * blockDim.x) {
-        const double one_f = 1.0 + (double)f[q];
         if (profile == TOMO_PROFILE_REF) {
-            const double r = 1500.0 * sqrt(one_f) * (double)kRefDT / (double)kRefH;
-            coef[q] = (float)(r * r);
-            rcoef[q] = (float)r;
+            const float v = rm(1500.f, __fsqrt_rn(ra(1.f, f[q])));
+            const float r = __fdiv_rn(rm(v, kRefDT), kRefH);
+            coef[q] = rm(r, r);
+            rcoef[q] = v;
         } else {
             const double c2 = (double)courant * (double)courant;
-            coef[q] = (float)(c2 * one_f);
+            coef[q] = (float)(c2 * (1.0 + (double)f[q]));
         }
     }
 }
 
-// One-way absorbing edge update of the reference at edge cell (i, j)
-// (sirt-mimo.cu:565-587).
+// One-way absorbing edge update of the reference at edge cell (i, j) (sirt-mimo.cu:565-587),
+// in its operation order: ((((2 - 2r - r r) u + 2r (1+r) ua) - r r ub) + (2r - 1) up) - 2r upa.
 __device__ __forceinline__ float ref_abc(const float* __restrict__ uc, const float* __restrict__ up,
                                          const float* __restrict__ rcoef, int i, int j, int nx, int ny) {
     const bool top = (j == 0), bottom = (j == ny - 1);
@@ -59,9 +67,14 @@ __device__ __forceinline__ float ref_abc(const float* __restrict__ uc, const flo
     const int ia = left ? i + 1 : right ? i - 1 : i;
     const int ib = left ? i + 2 : right ? i - 2 : i;
     const int64_t q = (int64_t)j * nx + i, qa = (int64_t)ja * nx + ia, qb = (int64_t)jb * nx + ib;
-    const float r = ldg(rcoef + q);
-    return (2.f - 2.f * r - r * r) * uc[q] + 2.f * r * (1.f + r) * uc[qa] - r * r * uc[qb] +
-           (2.f * r - 1.f) * up[q] - 2.f * r * up[qa];
+    const float r = __fdiv_rn(rm(ldg(rcoef + q), kRefDT), kRefH);
+    const float r2 = rm(r, r), tr = rm(2.f, r);
+    const float a1 = rm(rs(rs(2.f, tr), r2), uc[q]);
+    const float a2 = rm(rm(tr, ra(1.f, r)), uc[qa]);
+    const float a3 = rm(r2, uc[qb]);
+    const float a4 = rm(rs(tr, 1.f), up[q]);
+    const float a5 = rm(tr, up[qa]);
+    return rs(ra(rs(ra(a1, a2), a3), a4), a5);
 }
 
 // ---------------------------------------------------------------------------
@@ -80,11 +93,19 @@ __global__ void __launch_bounds__(BX * BY) k_fwd(DevGeo g, const float* __restri
     float val;
     if (PROF == TOMO_PROFILE_REF) {
         if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1) {
+            // r r (((E + W) + S) + N) + (2 - 4 r r) u - up (sirt-mimo.cu:532-541); 4 r r is exact
             const float r2 = ldg(coef + q);
-            val = r2 * (uc[q + 1] + uc[q - 1] + uc[q - nx] + uc[q + nx]) + (2.f - 4.f * r2) * uc[q] - up[q];
+            const float nb = ra(ra(ra(uc[q + 1], uc[q - 1]), uc[q - nx]), uc[q + nx]);
+            val = rs(ra(rm(r2, nb), rm(rs(2.f, rm(4.f, r2)), uc[q])), up[q]);
             if (s.k < g.n_src_steps) {                       // k + 1 <= 24 (sirt-mimo.cu:554)
                 const int32_t* b = g.box + 4 * (s.g0 + gl);
-                if (i >= b[0] && i <= b[1] && j >= b[2] && j <= b[3]) val += r2 * ldg(g.src + s.k);
+                if (i >= b[0] && i <= b[1] && j >= b[2] && j <= b[3]) {
+                    // v v DT DT cos(wc t) exp(-t^2 / 2 tau^2) (sirt-mimo.cu:555-560); the two FP32
+                    // factors come from the host's table (src[k], src[n_src_steps + k])
+                    const float v = ldg(rcoef + q);
+                    const float a = rm(rm(rm(rm(v, v), kRefDT), kRefDT), ldg(g.src + s.k));
+                    val = ra(val, rm(a, ldg(g.src + g.n_src_steps + s.k)));
+                }
             }
         } else if ((i == 0 || i == nx - 1) && (j == 0 || j == ny - 1)) {
             // corner: the mean of its two edge neighbours, which propagation_at_corners
@@ -126,22 +147,32 @@ __global__ void __launch_bounds__(BX * BY) k_fwd(DevGeo g, const float* __restri
 // thread evaluates backpropagation1 at its "source" cell.  The correlation
 // adds z(k) * Lu(k), Lu the clamped-edge Laplacian of u(k) with corner means
 // (laplace, laplace_corners); the 1/h^2 factor is applied by the update.
-__device__ __forceinline__ float ref_bp1(const float* __restrict__ c, const float* __restrict__ z1,
+// backpropagation1 at interior cell q (sirt-mimo.cu:697-707) in its operation order:
+// ((A ((((of_s z_s + of_n z_n) + of_w z_w) + of_e z_e) - 4 of z)) / h^2 + 2 z) - z2, with
+// A = (1500 1500)(DT DT) and of = 1 + f.
+__device__ __forceinline__ float ref_bp1(const float* __restrict__ f, const float* __restrict__ z1,
                                          const float* __restrict__ z2, int64_t q, int nx) {
-    return (ldg(c + q - nx) * z1[q - nx] + ldg(c + q + nx) * z1[q + nx] + ldg(c + q - 1) * z1[q - 1] +
-            ldg(c + q + 1) * z1[q + 1] - 4.f * ldg(c + q) * z1[q]) +
-           2.f * z1[q] - z2[q];
+    constexpr float A = (1500.f * 1500.f) * (kRefDT * kRefDT);
+    constexpr float HH = kRefH * kRefH;
+    const float s = ra(ra(ra(rm(ra(1.f, ldg(f + q - nx)), z1[q - nx]), rm(ra(1.f, ldg(f + q + nx)), z1[q + nx])),
+                          rm(ra(1.f, ldg(f + q - 1)), z1[q - 1])),
+                       rm(ra(1.f, ldg(f + q + 1)), z1[q + 1]));
+    const float l = rs(s, rm(rm(4.f, ra(1.f, ldg(f + q))), z1[q]));
+    return rs(ra(__fdiv_rn(rm(A, l), HH), rm(2.f, z1[q])), z2[q]);
 }
 
+// (((u_ja + u_jb) + u_ia) + u_ib) - 4 u with clamped edges (sirt-mimo.cu:786-803), unscaled
 __device__ __forceinline__ float clamped_lap(const float* __restrict__ u, int i, int j, int nx, int ny) {
     const int ja = j > 0 ? j - 1 : j, jb = j < ny - 1 ? j + 1 : j;
     const int ia = i > 0 ? i - 1 : i, ib = i < nx - 1 ? i + 1 : i;
-    return u[(int64_t)ja * nx + i] + u[(int64_t)jb * nx + i] + u[(int64_t)j * nx + ia] +
-           u[(int64_t)j * nx + ib] - 4.f * u[(int64_t)j * nx + i];
+    return rs(ra(ra(ra(u[(int64_t)ja * nx + i], u[(int64_t)jb * nx + i]), u[(int64_t)j * nx + ia]),
+                 u[(int64_t)j * nx + ib]),
+              rm(4.f, u[(int64_t)j * nx + i]));
 }
 
 template <int PROF>
-__global__ void __launch_bounds__(BX * BY) k_adj(DevGeo g, const float* __restrict__ coef, AdjStep s) {
+__global__ void __launch_bounds__(BX * BY) k_adj(DevGeo g, const float* __restrict__ coef,
+                                                 const float* __restrict__ fref, AdjStep s) {
     const int i = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int gl = blockIdx.z;
@@ -168,11 +199,11 @@ __global__ void __launch_bounds__(BX * BY) k_adj(DevGeo g, const float* __restri
         } else if (i == lo && j > lo && j < hi) {
             si = lo + 1; ch = 3 * nx + j;        // left
         }
-        val = ref_bp1(coef, z1, z2, (int64_t)sj * nx + si, nx);
-        if (ch >= 0) val += rr[ch] * 0.001f * 1000.f;     // rr * H * 1000 (sirt-mimo.cu:725-739)
+        val = ref_bp1(fref, z1, z2, (int64_t)sj * nx + si, nx);
+        if (ch >= 0) val = ra(val, rm(rm(rr[ch], kRefH), 1000.f));   // z + rr H 1000 (sirt-mimo.cu:725-739)
         if ((i == 0 || i == nx - 1) && (j == 0 || j == ny - 1)) {
             const int i1 = i == 0 ? 1 : nx - 2, j1 = j == 0 ? 1 : ny - 2;
-            lu = 0.5f * (clamped_lap(u, i, j1, nx, ny) + clamped_lap(u, i1, j, nx, ny));
+            lu = rm(0.5f, ra(clamped_lap(u, i, j1, nx, ny), clamped_lap(u, i1, j, nx, ny)));
         } else {
             lu = clamped_lap(u, i, j, nx, ny);
         }
@@ -427,10 +458,10 @@ void launch_fwd_step(int profile, const DevGeo& g, const float* coef, const floa
     else k_fwd<TOMO_PROFILE_CFG><<<grid, dim3(BX, BY), 0, S(st)>>>(g, coef, rcoef, s);
 }
 
-void launch_adj_step(int profile, const DevGeo& g, const float* coef, const AdjStep& s, void* st) {
+void launch_adj_step(int profile, const DevGeo& g, const float* coef, const float* f, const AdjStep& s, void* st) {
     dim3 grid((g.nx + BX - 1) / BX, (g.ny + BY - 1) / BY, s.ng);
-    if (profile == TOMO_PROFILE_REF) k_adj<TOMO_PROFILE_REF><<<grid, dim3(BX, BY), 0, S(st)>>>(g, coef, s);
-    else k_adj<TOMO_PROFILE_CFG><<<grid, dim3(BX, BY), 0, S(st)>>>(g, coef, s);
+    if (profile == TOMO_PROFILE_REF) k_adj<TOMO_PROFILE_REF><<<grid, dim3(BX, BY), 0, S(st)>>>(g, coef, f, s);
+    else k_adj<TOMO_PROFILE_CFG><<<grid, dim3(BX, BY), 0, S(st)>>>(g, coef, f, s);
 }
 
 void launch_gather(const DevGeo& g, const GatherStep& s, void* st) {

@@ -138,7 +138,7 @@ extern "C" tomo_status tomo_forward_noalloc(const tomo_config* cfg, const float*
     do {                                             \
         if ((e = (x)) != cudaSuccess) return cuda_fail(e, #x); \
     } while (0)
-    if ((s = put_words((uint32_t*)src, geo.src.data(), nt, st)) != TOMO_OK) return s;
+    if ((s = put_words((uint32_t*)src, geo.src.data(), (int64_t)geo.src.size(), st)) != TOMO_OK) return s;
     if ((s = put_words((uint32_t*)rcv, geo.rcv.data(), nch, st)) != TOMO_OK) return s;
     if (geo.ref) s = put_words((uint32_t*)box, geo.box.data(), 4 * (int64_t)geo.G, st);
     else s = put_words((uint32_t*)emit, geo.emit.data(), (int64_t)geo.G * geo.gs, st);

@@ -162,6 +162,10 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_forward_device": (i32, [vp, vp, vp]),
         "tomo_iterate_device": (i32, [vp, i32, C.POINTER(Schedule), i32, vp, vp, vp, C.POINTER(IterStats)]),
         "tomo_synchronize": (i32, [vp]),
+        "tomo_gradient_groups_device": (i32, [vp, vp, i32, i32, DP]),
+        "tomo_get_correlations_device": (i32, [vp, i32, i32, vp]),
+        "tomo_set_correlations_device": (i32, [vp, i32, i32, vp]),
+        "tomo_update_device": (i32, [vp, i32, C.POINTER(Schedule), i32, vp, vp, C.POINTER(IterStats)]),
         "tomo_time_kernel": (i32, [vp, i32, i32, DP, DP]),
         "tomo_forward_noalloc": (i32, [C.POINTER(Config), vp, vp, vp]),
         "tomo_net_num_params": (C.c_int64, []),
@@ -322,6 +326,26 @@ class Context:
         self._check(lib().tomo_iterate_device(self.h, method, C.byref(sched), it, C.c_void_p(d_f),
                                               C.c_void_p(d_rec or None), C.c_void_p(d_ftrue or None),
                                               C.byref(stats)))
+        return stats
+
+    def gradient_groups_device(self, d_f: int, g0: int, ng: int) -> float:
+        """Gradient sweeps of groups g0 .. g0+ng-1 for the device field d_f; their correlations stay
+        in the context.  Returns their squared record residual."""
+        r2 = C.c_double()
+        self._check(lib().tomo_gradient_groups_device(self.h, C.c_void_p(d_f), g0, ng, C.byref(r2)))
+        return r2.value
+
+    def get_correlations_device(self, g0: int, ng: int, d_out: int):
+        self._check(lib().tomo_get_correlations_device(self.h, g0, ng, C.c_void_p(d_out)))
+
+    def set_correlations_device(self, g0: int, ng: int, d_in: int):
+        self._check(lib().tomo_set_correlations_device(self.h, g0, ng, C.c_void_p(d_in)))
+
+    def update_device(self, method, sched, it, d_f: int, d_ftrue: int = 0):
+        """The update rule of a SIRT method from the correlations held for all groups."""
+        stats = IterStats()
+        self._check(lib().tomo_update_device(self.h, method, C.byref(sched), it, C.c_void_p(d_f),
+                                             C.c_void_p(d_ftrue or None), C.byref(stats)))
         return stats
 
     def time_kernel(self, which: int, steps: int):
