@@ -327,6 +327,21 @@ def time_to_image(ctx, w, sched, d_f, d_ft, torch, dev, plain_iters=30):
             "speedup": t_plain / t_learned if reached else None}
 
 
+def art_iteration(ctx, sched, d_f, d_ft, sirt_ms, iters=2):
+    """One ART iteration (art-mimo.cu:688-736: each group's gradient sweep and update in turn) on
+    the same workload, after one untimed iteration that captures the per-group graphs; reported
+    beside the SIRT iteration it is compared with."""
+    ctx.iterate_device(tomo.ART, sched, 0, d_f.data_ptr(), 0, d_ft.data_ptr())
+    ctx.synchronize()
+    ms = []
+    for it in range(1, 1 + iters):
+        st = ctx.iterate_device(tomo.ART, sched, it, d_f.data_ptr(), 0, d_ft.data_ptr())
+        ms.append(st.seconds * 1e3)
+    ms = min(ms)
+    return {"iteration_ms": ms, "sirt_iteration_ms": sirt_ms, "ratio_to_sirt": ms / sirt_ms,
+            "kernel_launches": st.kernel_launches}
+
+
 def max_over_ranks(x, dist, dev=None):
     """The largest x over all ranks (x itself without a process group)."""
     if not dist:
@@ -360,6 +375,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the time-to-image leg (c2)")
+    ap.add_argument("--no-art", action="store_true", help="skip the ART iteration leg (c2, c1)")
     ap.add_argument("--nt", type=int, default=0,
                     help="time steps instead of the workload's (small cases for profiling; the workload "
                          "name in the line says so)")
@@ -473,6 +489,8 @@ def main():
     d2h = 4 * fo.size + 8
 
     tti = time_to_image(ctx, w, sched, d_f, d_ft, torch, dev) if args.workload == "c2" and not args.no_learned else None
+    art = art_iteration(ctx, sched, d_f, d_ft, t_max / args.steps) if args.workload in ("c2", "c1") and not args.no_art \
+        else None
 
     # roofline of the dominant kernel, timed live on the context stream
     info = ctx.info
@@ -519,6 +537,8 @@ def main():
         }
         if tti is not None:
             line["time_to_image"] = tti
+        if art is not None:
+            line["art"] = art
         if cpu:
             line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         print(json.dumps(line), flush=True)

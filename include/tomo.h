@@ -246,8 +246,9 @@ tomo_status tomo_update_device(tomo_ctx* ctx, int32_t method, const tomo_schedul
                                float* d_f, const float* d_f_true, tomo_iter_stats* stats);
 
 /* Profiling hook (no reference counterpart): runs `steps` consecutive time steps
- * of one hot kernel for the first pass's groups on the context stream, bracketed
- * by CUDA events, after at least one tomo_iterate.  which: 0 forward step,
+ * of one hot kernel for the first pass's groups on the context stream, captured
+ * into a CUDA graph and replayed (as the iterations replay theirs), bracketed by
+ * CUDA events, after at least one tomo_iterate.  which: 0 forward step,
  * 1 adjoint step.  Returns the mean duration of one time step (kernels that
  * advance two steps per launch count as two) and the algorithmic bytes of one
  * step (16 B forward / 20 B adjoint per cell-update).

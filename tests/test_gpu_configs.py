@@ -96,7 +96,10 @@ def c2_phantom():
 KERNELS = {
     "autotuned": None,
     "fwd3208-adj3308": dict(TOMO_STRIP_ROWS="8", TOMO_FWD_ROWS="3208", TOMO_FWD_PAIR="0", TOMO_ADJ_PAIR="1",
-                            TOMO_ADJ_PAIR_ROWS="3308"),
+                            TOMO_ADJ_PAIR_ROWS="3308", TOMO_TILE="0"),
+    "fwd6008-adj7016": dict(TOMO_STRIP_ROWS="8", TOMO_FWD_ROWS="6008", TOMO_FWD_PAIR="0", TOMO_ADJ_PAIR="1",
+                            TOMO_ADJ_PAIR_ROWS="7016", TOMO_TILE="0"),
+    "tiles": dict(TOMO_STRIP_ROWS="8", TOMO_FWD_PAIR="0", TOMO_ADJ_PAIR="0", TOMO_TILE="1"),
 }
 
 _C2 = {}

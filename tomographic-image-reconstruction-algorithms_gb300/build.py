@@ -24,7 +24,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I" + INCLUDE, "-I" + CSRC]
 
-LIB_SOURCES = ["kernels.cu", "strip.cu", "engine.cu", "geometry.cpp", "noalloc.cu", "cnn.cu", "net.cu"]
+LIB_SOURCES = ["kernels.cu", "strip.cu", "tile.cu", "engine.cu", "geometry.cpp", "noalloc.cu", "cnn.cu", "net.cu"]
 # driver name -> -D selector of cli/tomo_cli.cpp
 DRIVERS = {
     "generate-field": "GENERATE_FIELD",
@@ -44,7 +44,7 @@ DRIVERS = {
     "sirt-mimo-norm-alt": "SIRT_MIMO_NORM_ALT",
     "tomo": "TOMO_MULTI",
 }
-HEADERS = [os.path.join(INCLUDE, "tomo.h"), os.path.join(CSRC, "internal.h")]
+HEADERS = [os.path.join(INCLUDE, "tomo.h"), os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "cell.cuh")]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

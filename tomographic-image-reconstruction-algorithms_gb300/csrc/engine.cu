@@ -62,6 +62,7 @@ struct tomo_ctx {
     uint32_t* rbits = nullptr;
     int rwords = 0;
     float* src = nullptr;
+    float* dmap = nullptr;       // CFG per-cell sponge factor
     uint8_t* mask = nullptr;
     int64_t bytes = 0;
     bool meas_set = false;
@@ -74,6 +75,9 @@ struct tomo_ctx {
     int rows_adj2 = 8;
     bool fwd_pair = false;       // two forward steps per launch (needs S >= 4)
     int rows_fwd2 = 8;
+    bool tile_fwd = false;       // multi-step tile kernels (tile.cu) for the forward sweeps
+    bool tile_adj = false;       // ... and for the adjoint sweeps
+    static constexpr int TILE_FWD_STEPS = 8;   // steps per forward tile launch
     // learned iteration (allocated on first use)
     float *illum = nullptr, *feat = nullptr, *fsave = nullptr, *dnet = nullptr, *dsave = nullptr;
     unsigned int *illum_max = nullptr, *maxsave = nullptr;
@@ -192,6 +196,44 @@ AdjStep adj_args(tomo_ctx* c, int q, int g0, int ng) {
     return as;
 }
 
+// Multi-step tile forward launch: slices k0+1 .. k0+T of the pass.
+TileFwd tile_fwd_args(tomo_ctx* c, int k0, int T, int g0, int ng) {
+    TileFwd a{};
+    a.hist = c->hist;
+    a.gstride = (int64_t)c->S * c->geo.N;
+    a.S = c->S;
+    a.k0 = k0;
+    a.T = T;
+    a.g0 = g0;
+    a.ng = ng;
+    a.K = std::max(c->K, 1);
+    a.nchunk = c->nchunk;
+    return a;
+}
+
+// Multi-step tile adjoint launch: z(kz0) .. z(kz0-T+1) of the pass (CFG: kz = q + 1).
+TileAdj tile_adj_args(tomo_ctx* c, int kz0, int T, int g0, int ng) {
+    const int64_t N = c->geo.N;
+    TileAdj a{};
+    a.z = c->z;
+    a.zstride = tomo_ctx::ZR * N;
+    a.hist = c->hist;
+    a.ustride = (int64_t)c->S * N;
+    a.S = c->S;
+    a.rr = c->rr;
+    a.rrstride = c->recs_per_group();
+    a.corr = c->corr + (int64_t)g0 * N;
+    a.cstride = N;
+    a.kz0 = kz0;
+    a.T = T;
+    a.ng = ng;
+    return a;
+}
+
+// Steps of the next tile adjoint launch when L steps remain: 6, 2 or 1 (the step counts whose
+// output slices miss the input slices' slots of the four-slot ring).
+int tile_adj_steps(int L) { return L >= 6 ? 6 : L >= 2 ? 2 : 1; }
+
 // Tuning cache line: problem key, then the choices.
 std::string tune_key(const tomo_ctx* c) {
     char b[160];
@@ -208,11 +250,14 @@ bool tune_cache_read(tomo_ctx* c, const char* path) {
     bool hit = false;
     while (!hit && std::fgets(line, sizeof line, fp)) {
         if (std::strncmp(line, key.c_str(), key.size()) != 0 || line[key.size()] != ' ') continue;
-        int v[7];
-        if (std::sscanf(line + key.size(), "%d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5],
-                        &v[6]) == 7) {
+        int v[9] = {0};
+        const int nv = std::sscanf(line + key.size(), "%d %d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3],
+                                   &v[4], &v[5], &v[6], &v[7], &v[8]);
+        if (nv == 7 || nv == 9) {
             c->rows_fwd = v[0]; c->rows_adj = v[1]; c->adj_variant = v[2]; c->adj_pair = v[3] != 0;
             c->rows_adj2 = v[4]; c->fwd_pair = v[5] != 0 && c->S >= 4; c->rows_fwd2 = v[6];
+            c->tile_fwd = v[7] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
+            c->tile_adj = v[8] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
             hit = true;
         }
     }
@@ -223,9 +268,20 @@ bool tune_cache_read(tomo_ctx* c, const char* path) {
 void tune_cache_append(const tomo_ctx* c, const char* path) {
     FILE* fp = std::fopen(path, "a");
     if (!fp) return;
-    std::fprintf(fp, "%s %d %d %d %d %d %d %d\n", tune_key(c).c_str(), c->rows_fwd, c->rows_adj, c->adj_variant,
-                 c->adj_pair ? 1 : 0, c->rows_adj2, c->fwd_pair ? 1 : 0, c->rows_fwd2);
+    std::fprintf(fp, "%s %d %d %d %d %d %d %d %d %d\n", tune_key(c).c_str(), c->rows_fwd, c->rows_adj,
+                 c->adj_variant, c->adj_pair ? 1 : 0, c->rows_adj2, c->fwd_pair ? 1 : 0, c->rows_fwd2,
+                 c->tile_fwd ? 1 : 0, c->tile_adj ? 1 : 0);
     std::fclose(fp);
+}
+
+// TOMO_TILE=0 / 1 / f / a turns the multi-step tile kernels off, on for both sweeps, on for the
+// forward or the adjoint sweeps only (tests and profiling).
+void tile_override(tomo_ctx* c) {
+    const char* e = std::getenv("TOMO_TILE");
+    if (!e || !*e) return;
+    const bool ok = tile_supported(c->dg, c->geo.cfg.profile);
+    c->tile_fwd = ok && (e[0] == '1' || e[0] == 'f');
+    c->tile_adj = ok && (e[0] == '1' || e[0] == 'a');
 }
 
 // Picks the strip kernels (rows per warp, register variant, one or two steps
@@ -247,6 +303,7 @@ tomo_status autotune(tomo_ctx* c) {
         if (const char* v = std::getenv("TOMO_FWD_PAIR")) c->fwd_pair = std::atoi(v) != 0 && c->S >= 4;
         c->rows_fwd2 = c->rows_fwd;
         if (const char* v = std::getenv("TOMO_FWD_PAIR_ROWS")) c->rows_fwd2 = std::atoi(v);
+        tile_override(c);
         return TOMO_OK;
     }
     const int cands[5] = {2, 4, 8, 16, 32};
@@ -303,8 +360,9 @@ tomo_status autotune(tomo_ctx* c) {
         // two steps per launch (reps/2 launches cover the same steps); codes as launch_adj2_strip
         for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows, 2000 + rows,
                          4000 + rows, 4100 + rows, 3200 + rows, 3300 + rows, 3400 + rows, 5200 + rows,
-                         5300 + rows}) {
-            if (code >= 5000 && rows < 16) continue;        // the 8-block staged build exists for rows 16, 32
+                         5300 + rows, 7000 + rows, 7100 + rows}) {
+            if (code >= 5000 && code < 7000 && rows < 16) continue;   // 8-block staged build: rows 16, 32
+            if (code >= 7000 && rows != 8 && rows != 16) continue;    // lean build: rows 8, 16
             if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {
@@ -323,7 +381,7 @@ tomo_status autotune(tomo_ctx* c) {
         }
     }
     // one-step forward with its inputs staged in shared memory
-    for (int code : {3204, 3208, 3216, 3304, 3308, 3316}) {
+    for (int code : {3204, 3208, 3216, 3304, 3308, 3316, 6004, 6008, 6016}) {
         if (code % 100 > 4 * c->geo.ny) continue;
         float ms = 1e30f;
         for (int pass = 0; pass < passes; ++pass) {
@@ -343,6 +401,33 @@ tomo_status autotune(tomo_ctx* c) {
     c->rows_fwd = rows_f1;
     c->rows_fwd2 = code_f2;
     c->fwd_pair = best_f2 < 0.97f * best_f1;
+    // multi-step tile kernels against the chosen strip kernels, per step: a forward launch of 8
+    // steps and adjoint launches of 6 + 2 steps
+    if (tile_supported(c->dg, c->geo.cfg.profile)) {
+        float ms_tf = 1e30f, ms_ta = 1e30f;
+        for (int pass = 0; pass < passes; ++pass) {
+            CU(c, cudaEventRecord(c->ev0, c->st));
+            launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, k0, reps, 0, ng), c->st);
+            CU(c, cudaEventRecord(c->ev1, c->st));
+            CU(c, cudaEventSynchronize(c->ev1));
+            float t_ms = 0.f;
+            CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+            if (pass > 0) ms_tf = std::min(ms_tf, t_ms);
+            CU(c, cudaEventRecord(c->ev0, c->st));
+            launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + reps + 1, 6, 0, ng), c->st);
+            launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + reps - 5, 2, 0, ng), c->st);
+            CU(c, cudaEventRecord(c->ev1, c->st));
+            CU(c, cudaEventSynchronize(c->ev1));
+            CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+            if (pass > 0) ms_ta = std::min(ms_ta, t_ms);
+        }
+        if (tlog)
+            std::fprintf(stderr, "tomo tune: tile forward %.2f us/step, tile adjoint %.2f us/step\n",
+                         1e3 * ms_tf / reps, 1e3 * ms_ta / reps);
+        c->tile_fwd = ms_tf < 0.97f * std::min(best_f1, c->fwd_pair ? best_f2 : best_f1);
+        c->tile_adj = ms_ta < 0.97f * best_a;
+    }
+    tile_override(c);
     CU(c, cudaGetLastError());
     if (cache && *cache) tune_cache_append(c, cache);
     return TOMO_OK;
@@ -355,7 +440,7 @@ tomo_status make_plan(tomo_ctx* c) {
     size_t free_b = 0, total_b = 0;
     CU(c, cudaMemGetInfo(&free_b, &total_b));
     // fixed buffers (fields, coefficients, accumulators, records)
-    const int64_t fixed = 4 * (6 * N) + 4 * (2 * G * N) + 4 * (2 * G * nt * g.nch) + 8 * (G * nt) +
+    const int64_t fixed = 4 * (7 * N) + 4 * (2 * G * N) + 4 * (2 * G * nt * g.nch) + 8 * (G * nt) +
                           8 * (int64_t)(G + 2) * reduce_blocks() + (int64_t)(64 << 20);
     const double budget = 0.90 * (double)free_b - (double)fixed;
     auto per_group = [&](bool full, int K) -> double {
@@ -421,6 +506,7 @@ tomo_status create_buffers(tomo_ctx* c) {
         TRY(c->alloc(&c->rid, N, "receiver map"));
         c->rwords = ((g.nx + 31) / 32 + 31) / 32;
         TRY(c->alloc(&c->rbits, (int64_t)g.ny * c->rwords, "receiver row bitmap"));
+        TRY(c->alloc(&c->dmap, N, "sponge map"));
     }
     CU(c, cudaMemsetAsync(c->rr, 0, sizeof(float) * P * nt * nch, c->st));
     CU(c, cudaMemsetAsync(c->meas, 0, sizeof(float) * G * nt * nch, c->st));
@@ -450,6 +536,18 @@ tomo_status create_buffers(tomo_ctx* c) {
     fill_damp(d);
     d.box = c->box; d.emit = c->emit; d.rcv = c->rcv; d.rid = c->rid; d.rbits = c->rbits; d.rwords = c->rwords; d.src = c->src;
     d.n_src_steps = g.n_src_steps;
+    if (!g.ref) {
+        // per-cell sponge factor: the damp table by distance to the nearest edge
+        std::vector<float> dm((size_t)N, 1.f);
+        for (int j = 0; j < g.ny; ++j)
+            for (int i = 0; i < g.nx; ++i) {
+                const int dd = std::min(std::min(i, j), std::min(g.nx - 1 - i, g.ny - 1 - j));
+                if (dd < d.sponge_w) dm[(size_t)j * g.nx + i] = d.damp[dd];
+            }
+        CU(c, cudaMemcpyAsync(c->dmap, dm.data(), sizeof(float) * N, cudaMemcpyHostToDevice, c->st));
+        CU(c, cudaStreamSynchronize(c->st));   // `dm` is local
+        d.dmap = c->dmap;
+    }
     c->strip = strip_supported(d, g.cfg.profile) && !std::getenv("TOMO_NO_STRIP");
     CU(c, cudaMemsetAsync(c->hist, 0, sizeof(float) * (size_t)P * c->S * N, c->st));
     CU(c, cudaMemsetAsync(c->z, 0, sizeof(float) * (size_t)P * tomo_ctx::ZR * N, c->st));
@@ -491,8 +589,28 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             fs.ckstride = (int64_t)c->nchunk * 2 * N;
         }
     };
+    if (c->tile_fwd) {
+        // multi-step tile launches: every slice 2 .. nt-1 is recorded by the launch computing it
+        for (int k = 1; k <= nt - 2;) {
+            const int T = std::min(tomo_ctx::TILE_FWD_STEPS, nt - 1 - k);
+            TileFwd a = tile_fwd_args(c, k, T, g0, ng);
+            if (mode == MODE_GRAD && !c->full) {
+                a.ckpt = c->ckpt;
+                a.ckstride = (int64_t)c->nchunk * 2 * N;
+            }
+            a.gmeas = resid ? meas_g : nullptr;
+            a.gout = out_g;
+            launch_fwd_tile(c->dg, c->coef, a, st);
+            ++n;
+            k += T;
+        }
+        if (resid) {
+            launch_resid_parts(c->rr, ng, nt, (int)nch, c->rpart + (int64_t)g0 * nt, st);
+            ++n;
+        }
+    }
     int gnext = 2;   // strip path: slices 2 .. gnext-1 are recorded, in order
-    for (int k = 1; k <= nt - 2;) {
+    for (int k = 1; k <= nt - 2 && !c->tile_fwd;) {
         FwdStep fs = fwd_args(c, k, g0, ng);
         const int m = k + 1;
         ck_of(fs, m);
@@ -533,7 +651,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         n += 2;
         k += 1;
     }
-    if (c->strip) {
+    if (c->strip && !c->tile_fwd) {
         for (int m = std::max(gnext, 2); m < nt - 1; ++m) {   // slices left before the last
             GatherStep gs{};
             gs.g0 = g0;
@@ -547,7 +665,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             ++n;
         }
     }
-    if (c->strip) {
+    if (c->strip && !c->tile_fwd) {
         GatherStep gs{};
         gs.g0 = g0;
         gs.u = c->hist + c->slot(nt - 1);
@@ -584,7 +702,11 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
                                        N, st);
                 }
                 for (int m = qa + 1; m <= qb;) {
-                    if (c->strip && c->fwd_pair && m + 1 <= qb) {
+                    if (c->tile_fwd) {
+                        const int T = std::min(tomo_ctx::TILE_FWD_STEPS, qb - m + 1);
+                        launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, m - 1, T, g0, ng), st);
+                        m += T;
+                    } else if (c->strip && c->fwd_pair && m + 1 <= qb) {
                         launch_fwd2_strip(c->rows_fwd2, c->dg, c->coef, fwd_args(c, m - 1, g0, ng),
                                           fwd_args(c, m, g0, ng), false, false, st);
                         m += 2;
@@ -597,7 +719,11 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             }
         }
         for (int q = qb; q >= qa;) {
-            if (c->adj_pair && q - 1 >= qa) {
+            if (c->tile_adj) {
+                const int T = tile_adj_steps(q - qa + 1);
+                launch_adj_tile(c->dg, c->coef, tile_adj_args(c, q + 1, T, g0, ng), st);
+                q -= T;
+            } else if (c->adj_pair && q - 1 >= qa) {
                 launch_adj2_strip(c->rows_adj2, c->dg, c->coef, adj_args(c, q, g0, ng), adj_args(c, q - 1, g0, ng), st);
                 q -= 2;
             } else {
@@ -1413,9 +1539,20 @@ tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* 
     const int k0 = std::max(2, (nt - steps) / 2);
     launch_coef(prof, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
     TRY(autotune(c));
-    CU(c, cudaEventRecord(c->ev0, c->st));
+    // the steps are captured into a graph and replayed, as the iterations run them, so the time
+    // per step carries the launch gaps of graph replay, not of stream launches
+    cudaGraph_t graph = nullptr;
+    CU(c, cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
     for (int t = 0; t < steps;) {
-        if (which == 0 && c->fwd_pair && t + 1 < steps) {
+        if (which == 0 && c->tile_fwd) {
+            const int T = std::min(tomo_ctx::TILE_FWD_STEPS, steps - t);
+            launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, k0 + t, T, 0, ng), c->st);
+            t += T;
+        } else if (which == 1 && c->tile_adj) {
+            const int T = tile_adj_steps(steps - t);
+            launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + steps - t, T, 0, ng), c->st);
+            t += T;
+        } else if (which == 0 && c->fwd_pair && t + 1 < steps) {
             launch_fwd2_strip(c->rows_fwd2, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), fwd_args(c, k0 + t + 1, 0, ng),
                               false, false, c->st);
             t += 2;
@@ -1431,11 +1568,25 @@ tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* 
             t += 1;
         }
     }
-    CU(c, cudaEventRecord(c->ev1, c->st));
-    CU(c, cudaEventSynchronize(c->ev1));
-    CU(c, cudaGetLastError());
+    const cudaError_t ec = cudaStreamEndCapture(c->st, &graph);
+    if (ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return c->cuda(ec, "cudaStreamEndCapture");
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) return c->cuda(ei, "cudaGraphInstantiate");
     float ms = 0.f;
-    CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    cudaError_t e = cudaGraphLaunch(exec, c->st);     // warm-up replay
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->st);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->st);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    cudaGraphExecDestroy(exec);
+    CU(c, e);
+    CU(c, cudaGetLastError());
     *ms_per_launch = (double)ms / steps;
     if (bytes_per_launch) *bytes_per_launch = (which == 0 ? 16.0 : 20.0) * (double)ng * (double)N;
     return TOMO_OK;

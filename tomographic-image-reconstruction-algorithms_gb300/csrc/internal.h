@@ -132,6 +132,7 @@ struct DevGeo {
     const int32_t* rid;    // CFG per-cell channel or -1
     const uint32_t* rbits; // CFG per row: bit b set when cells [32b, 32b+32) hold a receiver
     int rwords;            // words of rbits per row
+    const float* dmap;     // CFG per-cell sponge factor (the damp table by edge distance), or null
     const float* src;      // source table (Geometry::src)
     int n_src_steps;
     // residual noise: simulated samples u become u * noise_factor(*noise_key, noise_level, ...)
@@ -243,5 +244,38 @@ void launch_fwd2_strip(int rows, const DevGeo& g, const float* coef, const FwdSt
 void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjStep& a, const AdjStep& b,
                        void* stream);
 void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, void* stream);
+
+// multi-step tile kernels (tile.cu): CFG profile with a receiver map.  A forward launch computes
+// slices k0+1 .. k0+T (T <= 8) of every group of the pass, writes each to its slot, its
+// checkpoint copy and its records; an adjoint launch computes z(kz0) .. z(kz0-T+1) (T in
+// {1, 2, 6}) with the correlation, writing the last two slices to the ring.
+struct TileFwd {
+    float* hist;         // forward slots of pass-group 0; slice m at slot m % S
+    int64_t gstride;
+    int S;
+    int k0, T;
+    int g0, ng;
+    float* ckpt;         // checkpoint copies (null: none): chunk ch >= 1 keeps slices ch K - 1 .. ch K
+    int64_t ckstride;
+    int K, nchunk;
+    const float* gmeas;  // measured records of pass-group 0 (null: simulate)
+    float* gout;         // records / residual of pass-group 0 (slices >= 2)
+};
+struct TileAdj {
+    float* z;            // adjoint ring of pass-group 0: z(m) at slot m % 4
+    int64_t zstride;
+    const float* hist;   // forward slots of pass-group 0: u(m-1) at slot (m-1) % S
+    int64_t ustride;
+    int S;
+    const float* rr;     // residual records of pass-group 0: step m at rr + m * nch
+    int64_t rrstride;
+    float* corr;         // correlation of pass-group 0
+    int64_t cstride;
+    int kz0, T;
+    int ng;
+};
+bool tile_supported(const DevGeo& g, int profile);
+void launch_fwd_tile(const DevGeo& g, const float* coef, const TileFwd& a, void* stream);
+void launch_adj_tile(const DevGeo& g, const float* coef, const TileAdj& a, void* stream);
 
 }  // namespace tomo

@@ -22,6 +22,8 @@
 namespace tomo {
 namespace {
 
+#include "cell.cuh"
+
 constexpr int BX = 32;
 constexpr int BY = 8;
 constexpr int RED_BLOCKS = 304;   // 2 x 152 SMs
@@ -116,22 +118,14 @@ __global__ void __launch_bounds__(BX * BY) k_fwd(DevGeo g, const float* __restri
             val = ref_abc(uc, up, rcoef, i, j, nx, ny);
         }
     } else {
-        const float c = ldg(coef + q);
-        const float u0 = uc[q];
+        // the strip kernels' cell arithmetic (cell.cuh), so every CFG path gives the same bits
         const float e = i + 1 < nx ? uc[q + 1] : 0.f;
         const float w = i > 0 ? uc[q - 1] : 0.f;
         const float so = j > 0 ? uc[q - nx] : 0.f;
         const float no = j + 1 < ny ? uc[q + nx] : 0.f;
-        const float lap = (e + w + so + no) - 4.f * u0;
-        const int dd = min(min(i, j), min(nx - 1 - i, ny - 1 - j));
-        const float d = dd < g.sponge_w ? g.damp[dd] : 1.f;
-        val = d * ((2.f * u0 - up[q]) + c * lap);
-        if (s.k < g.n_src_steps) {
-            const int32_t* em = g.emit + (int64_t)(s.g0 + gl) * g.gs;
-            const float a = ldg(g.src + s.k);
-            for (int e2 = 0; e2 < g.gs; ++e2)
-                if (em[e2] == q) val += a;
-        }
+        const float a = s.k < g.n_src_steps ? emit_at(g.emit + (int64_t)(s.g0 + gl) * g.gs, g.gs, q, ldg(g.src + s.k))
+                                            : 0.f;
+        val = fwd_cell(e, w, so, no, uc[q], up[q], ldg(coef + q), sponge(g, i, j), a);
     }
     s.un[gl * s.gstride + q] = val;
     if (s.ck) s.ck[gl * s.ckstride + q] = val;
@@ -210,26 +204,22 @@ __global__ void __launch_bounds__(BX * BY) k_adj(DevGeo g, const float* __restri
     } else {
         // CFG: exact discrete adjoint z(m) = d((2 z1 - z2) + Lap(c z1) + inj),
         // correlation with the zero-padded Laplacian of u(m-1).
-        const float c0 = ldg(coef + q);
-        const float e = i + 1 < nx ? ldg(coef + q + 1) * z1[q + 1] : 0.f;
-        const float w = i > 0 ? ldg(coef + q - 1) * z1[q - 1] : 0.f;
-        const float so = j > 0 ? ldg(coef + q - nx) * z1[q - nx] : 0.f;
-        const float no = j + 1 < ny ? ldg(coef + q + nx) * z1[q + nx] : 0.f;
-        const float lz = (e + w + so + no) - 4.f * c0 * z1[q];
+        const float e = i + 1 < nx ? mul(ldg(coef + q + 1), z1[q + 1]) : 0.f;
+        const float w = i > 0 ? mul(ldg(coef + q - 1), z1[q - 1]) : 0.f;
+        const float so = j > 0 ? mul(ldg(coef + q - nx), z1[q - nx]) : 0.f;
+        const float no = j + 1 < ny ? mul(ldg(coef + q + nx), z1[q + nx]) : 0.f;
         const int r = g.rid[q];
         const float inj = r >= 0 ? rr[r] : 0.f;
-        const int dd = min(min(i, j), min(nx - 1 - i, ny - 1 - j));
-        const float d = dd < g.sponge_w ? g.damp[dd] : 1.f;
-        val = d * ((2.f * z1[q] - z2[q]) + lz + inj);
+        val = adj_cell(e, w, so, no, mul(ldg(coef + q), z1[q]), z1[q], z2[q], inj, sponge(g, i, j));
         const float ue = i + 1 < nx ? u[q + 1] : 0.f;
         const float uw = i > 0 ? u[q - 1] : 0.f;
         const float us = j > 0 ? u[q - nx] : 0.f;
         const float un = j + 1 < ny ? u[q + nx] : 0.f;
-        lu = (ue + uw + us + un) - 4.f * u[q];
+        lu = lap5(ue, uw, us, un, u[q]);
     }
     s.zk[gl * s.zstride + q] = val;
     float* cr = s.corr + gl * s.cstride + q;
-    *cr += val * lu;
+    *cr = __fmaf_rn(val, lu, *cr);
 }
 
 // ---------------------------------------------------------------------------

@@ -23,99 +23,10 @@
 namespace tomo {
 namespace {
 
-constexpr unsigned FULL = 0xffffffffu;
+#include "cell.cuh"
+
 constexpr int STRIP = 128;     // cells per warp strip
 constexpr int WARPS = 4;       // warps per block (stacked in y)
-
-__device__ __forceinline__ float4 ld4(const float* __restrict__ p, int64_t off, bool ok) {
-    return ok ? *reinterpret_cast<const float4*>(p + off) : make_float4(0.f, 0.f, 0.f, 0.f);
-}
-
-// Sponge factor of cell (i, j): a table lookup by the distance to the nearest edge.
-__device__ __forceinline__ float sponge(const DevGeo& g, int i, int j) {
-    const int dd = min(min(i, j), min(g.nx - 1 - i, g.ny - 1 - j));
-    return dd < g.sponge_w ? g.damp[dd] : 1.f;
-}
-
-// Adjoint arithmetic with explicit rounding: the one-step and two-step kernels
-// evaluate every cell with these, so their results agree bit for bit whatever
-// the compiler would otherwise contract into fused multiply-adds.
-__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-
-// Packed FP32x2 arithmetic (add/sub/mul/fma .rn.f32x2, sm_100 and later): one instruction for
-// a lane's two cells, each half rounded exactly as the scalar __fadd_rn / __fsub_rn /
-// __fmul_rn / __fmaf_rn, so results match the one-cell helpers bit for bit.
-__device__ __forceinline__ float2 pk_add(float2 a, float2 b) {
-    float2 r;
-    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-__device__ __forceinline__ float2 pk_sub(float2 a, float2 b) {
-    float2 r;
-    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-__device__ __forceinline__ float2 pk_mul(float2 a, float2 b) {
-    float2 r;
-    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c) {
-    float2 r;
-    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return r;
-}
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return make_float2(mul(a.x, b.x), mul(a.y, b.y)); }
-__device__ __forceinline__ float4 mul4(float4 a, float4 b) {
-    return make_float4(mul(a.x, b.x), mul(a.y, b.y), mul(a.z, b.z), mul(a.w, b.w));
-}
-
-// d * ((2 z - z2) + ((((ce + cw) + cs) + cn) - 4 cz) + inj), where cz = c z and the
-// neighbour products c z are passed in rounded (4 cz is exact: a power-of-two scale)
-__device__ __forceinline__ float adj_cell(float ce, float cw, float cs, float cn, float cz, float z, float z2,
-                                          float inj, float d) {
-    const float lz = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(ce, cw), cs), cn), mul(4.f, cz));
-    return mul(d, __fadd_rn(__fadd_rn(__fsub_rn(mul(2.f, z), z2), lz), inj));
-}
-
-// ((e + w) + s) + n - 4 u
-__device__ __forceinline__ float lap5(float e, float w, float s, float n, float u) {
-    return __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(e, w), s), n), mul(4.f, u));
-}
-
-// adj_cell and lap5 for a lane's two cells in packed FP32x2 (same operation order)
-__device__ __forceinline__ float2 adj_cell2(float2 ce, float2 cw, float2 cs, float2 cn, float2 cz, float2 z, float2 z2,
-                                            float2 inj, float2 d) {
-    const float2 lz = pk_sub(pk_add(pk_add(pk_add(ce, cw), cs), cn), pk_mul(make_float2(4.f, 4.f), cz));
-    return pk_mul(d, pk_add(pk_add(pk_sub(pk_mul(make_float2(2.f, 2.f), z), z2), lz), inj));
-}
-__device__ __forceinline__ float2 lap5_2(float2 e, float2 w, float2 s, float2 n, float2 u) {
-    return pk_sub(pk_add(pk_add(pk_add(e, w), s), n), pk_mul(make_float2(4.f, 4.f), u));
-}
-
-// Forward cell update d * ((2 u - up) + c * lap) + a, explicit rounding (shared by
-// the one-step and two-step forward kernels).
-__device__ __forceinline__ float fwd_cell(float e, float w, float s, float n, float u, float up, float c, float d,
-                                          float a) {
-    const float v = __fadd_rn(__fsub_rn(mul(2.f, u), up), mul(c, lap5(e, w, s, n, u)));
-    return __fadd_rn(mul(d, v), a);
-}
-
-// Source amplitude a at cell q of group g at step k (0 when q emits nothing).
-__device__ __forceinline__ float emit_at(const int32_t* em, int gs, int64_t q, float a) {
-    float r = 0.f;
-    for (int t = 0; t < gs; ++t)
-        if (em[t] == q) r += a;
-    return r;
-}
 
 // West neighbour of element 0 and east neighbour of element 3 of each lane.
 __device__ __forceinline__ void we(const float4& v, const float* __restrict__ row, int lane, int x0, int nx,
@@ -124,49 +35,6 @@ __device__ __forceinline__ void we(const float4& v, const float* __restrict__ ro
     east = __shfl_down_sync(FULL, v.x, 1);
     if (lane == 0) west = x0 > 0 ? row[x0 - 1] : 0.f;
     if (lane == 31) east = x0 + STRIP < nx ? row[x0 + STRIP] : 0.f;
-}
-
-// Receiver bitmap (g.rbits: per row, one bit per 32-cell block, g.rwords words per row) words
-// and masks covering a strip's cells [xa, xb); a strip of at most 128 cells spans at most two
-// words.  Strips whose rows have no receiver never read the per-cell receiver map.
-struct RcvMask {
-    int w0, w1;
-    uint32_t m0, m1;
-};
-
-__device__ __forceinline__ RcvMask rcv_mask(const DevGeo& g, int xa, int xb) {
-    xa = max(xa, 0);
-    xb = min(xb, g.nx);
-    RcvMask k{0, 0, 0u, 0u};
-    if (xa >= xb) return k;
-    const int b0 = xa >> 5, b1 = (xb - 1) >> 5;
-    k.w0 = b0 >> 5;
-    k.w1 = b1 >> 5;
-    const uint32_t lo = ~0u << (b0 & 31);
-    const uint32_t hi = (b1 & 31) == 31 ? ~0u : ((1u << ((b1 & 31) + 1)) - 1u);
-    if (k.w0 == k.w1) {
-        k.m0 = lo & hi;
-    } else {
-        k.m0 = lo;
-        k.m1 = hi;
-    }
-    return k;
-}
-
-// Whether row r has a receiver in the strip (the same answer for the whole warp).
-__device__ __forceinline__ bool rcv_row(const DevGeo& g, const RcvMask& k, int r) {
-    if (r < 0 || r >= g.ny) return false;
-    const uint32_t* w = g.rbits + (int64_t)r * g.rwords;
-    return ((w[k.w0] & k.m0) | (k.m1 ? (w[k.w1] & k.m1) : 0u)) != 0u;
-}
-
-// Distance of index i to the nearer end of [0, n), clamped at 0 for indices outside.
-__device__ __forceinline__ int edge_dist(int i, int n) { return max(0, min(i, n - 1 - i)); }
-
-// Sponge factor from a cell's column and row edge distances (equal to sponge(g, i, j)).
-__device__ __forceinline__ float damp_at(const DevGeo& g, int dcol, int drow) {
-    const int dd = min(dcol, drow);
-    return dd < g.sponge_w ? g.damp[dd] : 1.f;
 }
 
 // ---------------------------------------------------------------------------
@@ -905,6 +773,140 @@ void adj2s_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStre
 }
 
 // ---------------------------------------------------------------------------
+// Two adjoint steps per launch, lean form: four cells per lane, 128-cell strips overlapping by
+// one lane (4 cells) on each side (lanes 1..30, 120 cells, write; lanes 0 and 31 compute the
+// first step as halo), rows y0-1 .. y0+R in a fully unrolled loop with every access predicated,
+// the sponge factor from the per-cell map, receiver rows flagged by two ballots at kernel start.
+// Rolling state and cell arithmetic are those of k_adj2_strip, so the results are identical.
+template <int R, int MB>
+__global__ void __launch_bounds__(WARPS * 32, MB) k_adjl2_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 120 - 4;
+    const int i = x0 + 4 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    const bool in = i >= 0 && i < nx;                // nx % 4 == 0: a lane's four cells are all in or out
+    const bool own = in && lane >= 1 && lane <= 30;
+    const float* __restrict__ z1 = s.z1 + gl * s.zstride;
+    const float* __restrict__ z2 = s.z2 + gl * s.zstride;
+    float* __restrict__ za = s.za + gl * s.zstride;
+    float* __restrict__ zb = s.zb + gl * s.zstride;
+    const float* __restrict__ ua = s.ua + gl * s.ustride;
+    const float* __restrict__ ub = s.ub + gl * s.ustride;
+    const float* __restrict__ rra = s.rra + gl * s.rrstride;
+    const float* __restrict__ rrb = s.rrb + gl * s.rrstride;
+    float* __restrict__ corr = s.corr + gl * s.cstride;
+    const float* __restrict__ dmap = g.dmap;
+    // receiver flags of rows y0-1 .. y0+R (R + 2 <= 64)
+    const RcvMask rk = rcv_mask(g, x0, x0 + STRIP);
+    const unsigned rb_lo = __ballot_sync(FULL, rcv_row(g, rk, y0 - 1 + lane));
+    const unsigned rb_hi = R + 2 > 32 ? __ballot_sync(FULL, rcv_row(g, rk, y0 + 31 + lane)) : 0u;
+    const unsigned long long rbits = ((unsigned long long)rb_hi << 32) | rb_lo;
+    auto row_in = [&](int r) { return in && r >= 0 && r < ny; };
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    // state at the top of iteration t (first step at row r = y0-1+t, second at row r-1):
+    // z(kz+1) rows r-1, r; c z(kz+1) rows r-1, r; the coefficient row r; z(kz) row r-1 and
+    // c z(kz) rows r-2, r-1; u(q), u(q-1) rows r-2, r-1; sponge and receivers of row r-1
+    int o = (y0 - 1) * nx;                            // offset of row r (32-bit: nx*ny < 2^31)
+    float4 z1m = ld4(z1, o - nx + i, row_in(y0 - 2));
+    float4 z10 = ld4(z1, o + i, row_in(y0 - 1));
+    float4 pzm = mul4(ld4(coef, o - nx + i, row_in(y0 - 2)), z1m);
+    float4 c0 = ld4(coef, o + i, row_in(y0 - 1));
+    float4 pz0 = mul4(c0, z10);
+    float4 zam = zero, pam2 = zero, pam = zero, uam2 = zero, uam = zero, ubm2 = zero, ubm = zero, dm = zero;
+    int4 ridm = make_int4(-1, -1, -1, -1);
+    bool rcvm = false;
+#pragma unroll
+    for (int t = 0; t < R + 2; ++t) {
+        const int r = y0 - 1 + t;
+        if (r > ny) break;                            // uniform per warp
+        const bool okr = row_in(r), okp = row_in(r + 1);
+        const float4 z1p = ld4(z1, o + nx + i, okp);
+        const float4 cp = ld4(coef, o + nx + i, okp);
+        const float4 zz = ld4(z2, o + i, okr);
+        const float4 ua0 = ld4(ua, o + i, okr);
+        const float4 ub0 = ld4(ub, o + i, okr);
+        const float4 d0 = ld4(dmap, o + i, okr);
+        const bool rcv = (rbits >> t) & 1ull;
+        int4 rid = make_int4(-1, -1, -1, -1);
+        if (rcv && okr) rid = *reinterpret_cast<const int4*>(g.rid + o + i);
+        const float4 pzp = mul4(cp, z1p);
+        // ---- first step: z(kz) at row r (zero outside the grid)
+        float4 za0 = zero;
+        {
+            const float pw = __shfl_up_sync(FULL, pz0.w, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
+            if (okr) {
+                float4 inj = zero;
+                if (rcv) {
+                    inj.x = rid.x >= 0 ? rra[rid.x] : 0.f;
+                    inj.y = rid.y >= 0 ? rra[rid.y] : 0.f;
+                    inj.z = rid.z >= 0 ? rra[rid.z] : 0.f;
+                    inj.w = rid.w >= 0 ? rra[rid.w] : 0.f;
+                }
+                za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, inj.x, d0.x);
+                za0.y = adj_cell(pz0.z, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, inj.y, d0.y);
+                za0.z = adj_cell(pz0.w, pz0.y, pzm.z, pzp.z, pz0.z, z10.z, zz.z, inj.z, d0.z);
+                za0.w = adj_cell(pe, pz0.z, pzm.w, pzp.w, pz0.w, z10.w, zz.w, inj.w, d0.w);
+            }
+        }
+        const float4 pa0 = mul4(c0, za0);
+        // ---- second step: z(kz-1) at row r-1, correlation of both steps at row r-1
+        {
+            const float pw = __shfl_up_sync(FULL, pam.w, 1), pe = __shfl_down_sync(FULL, pam.x, 1);
+            const float uaw = __shfl_up_sync(FULL, uam.w, 1), uae = __shfl_down_sync(FULL, uam.x, 1);
+            const float ubw = __shfl_up_sync(FULL, ubm.w, 1), ube = __shfl_down_sync(FULL, ubm.x, 1);
+            if (t >= 2 && own && r - 1 < ny) {
+                const int ob = o - nx;
+                float4 inj = zero;
+                if (rcvm) {
+                    inj.x = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
+                    inj.y = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
+                    inj.z = ridm.z >= 0 ? rrb[ridm.z] : 0.f;
+                    inj.w = ridm.w >= 0 ? rrb[ridm.w] : 0.f;
+                }
+                float4 zbv;
+                zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, inj.x, dm.x);
+                zbv.y = adj_cell(pam.z, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, inj.y, dm.y);
+                zbv.z = adj_cell(pam.w, pam.y, pam2.z, pa0.z, pam.z, zam.z, z1m.z, inj.z, dm.z);
+                zbv.w = adj_cell(pe, pam.z, pam2.w, pa0.w, pam.w, zam.w, z1m.w, inj.w, dm.w);
+                float4 cr = *reinterpret_cast<const float4*>(corr + ob + i);
+                cr.x = __fmaf_rn(zam.x, lap5(uam.y, uaw, uam2.x, ua0.x, uam.x), cr.x);
+                cr.y = __fmaf_rn(zam.y, lap5(uam.z, uam.x, uam2.y, ua0.y, uam.y), cr.y);
+                cr.z = __fmaf_rn(zam.z, lap5(uam.w, uam.y, uam2.z, ua0.z, uam.z), cr.z);
+                cr.w = __fmaf_rn(zam.w, lap5(uae, uam.z, uam2.w, ua0.w, uam.w), cr.w);
+                cr.x = __fmaf_rn(zbv.x, lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x), cr.x);
+                cr.y = __fmaf_rn(zbv.y, lap5(ubm.z, ubm.x, ubm2.y, ub0.y, ubm.y), cr.y);
+                cr.z = __fmaf_rn(zbv.z, lap5(ubm.w, ubm.y, ubm2.z, ub0.z, ubm.z), cr.z);
+                cr.w = __fmaf_rn(zbv.w, lap5(ube, ubm.z, ubm2.w, ub0.w, ubm.w), cr.w);
+                *reinterpret_cast<float4*>(corr + ob + i) = cr;
+                *reinterpret_cast<float4*>(za + ob + i) = zam;
+                *reinterpret_cast<float4*>(zb + ob + i) = zbv;
+            }
+        }
+        z1m = z10; z10 = z1p;
+        pzm = pz0; pz0 = pzp;
+        c0 = cp;
+        zam = za0;
+        pam2 = pam; pam = pa0;
+        uam2 = uam; uam = ua0;
+        ubm2 = ubm; ubm = ub0;
+        dm = d0;
+        ridm = rid;
+        rcvm = rcv;
+        o += nx;
+    }
+}
+
+template <int R, int MB>
+void adjl2_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    dim3 grid((g.nx + 119) / 120, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
+    k_adjl2_strip<R, MB><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+}
+
+// ---------------------------------------------------------------------------
 // Two forward steps per launch.  Same strip geometry as k_adj2_strip (2 cells
 // per lane, 64-cell strips overlapping by one lane each side, lanes 1..30
 // write).  u(k+1) rows y0-1 .. y0+R roll through registers and u(k+2) follows
@@ -1358,6 +1360,97 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_fwds_strip(DevGeo g, const fl
     cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// One forward step, lean form: four cells per lane (128-cell strips), R rows per warp in a fully
+// unrolled loop with every access predicated instead of branched, the sponge factor from the
+// per-cell map (one 128-bit load per row instead of per-cell edge-distance lookups), the source
+// term only in launches of source steps (SRC), the west / east neighbours of a lane's four cells
+// by shuffles with one predicated scalar load at each strip end.  Same cell arithmetic
+// (fwd_cell) as every other forward kernel, so the same bits.
+template <int R, bool SRC>
+__global__ void __launch_bounds__(WARPS * 32, 8) k_fwdl_strip(DevGeo g, const float* __restrict__ coef, FwdStep s) {
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    if (blockIdx.y == gridDim.y - 1) {
+        // sensor gather of slice k (k >= 2), one block per group
+        if (blockIdx.x != 0 || s.gk < 2) return;
+        const float* u = s.uc + gl * s.gstride;
+        const int64_t base = ((int64_t)gl * g.nt + s.gk) * g.nch;
+        const bool noisy = s.gmeas && g.noise_key;
+        const uint64_t key = noisy ? *g.noise_key : 0;
+        for (int c = threadIdx.x; c < g.nch; c += blockDim.x) {
+            const int cell = g.rcv[c];
+            float v = cell >= 0 ? u[cell] : 0.f;
+            if (noisy) v *= noise_factor(key, g.noise_level, s.g0 + gl, s.gk, c);
+            s.gout[base + c] = s.gmeas ? (cell >= 0 ? s.gmeas[base + c] - v : 0.f) : v;
+        }
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * STRIP;
+    const int i = x0 + 4 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    const bool act = i < nx;                         // nx % 4 == 0: a lane's four cells are all in or out
+    const float* __restrict__ uc = s.uc + gl * s.gstride;
+    const float* __restrict__ up = s.up + gl * s.gstride;
+    float* __restrict__ un = s.un + gl * s.gstride;
+    float* __restrict__ ck = s.ck ? s.ck + gl * s.ckstride : nullptr;
+    const float* __restrict__ dmap = g.dmap;
+    // lane 0 reads the cell west of the strip, lane 31 the cell east of it
+    const int xs = lane == 0 ? x0 - 1 : x0 + STRIP;
+    const bool side = (lane == 0 && x0 > 0) || (lane == 31 && x0 + STRIP < nx);
+    const int ggl = s.g0 + gl;
+    const float a = SRC ? g.src[s.k] : 0.f;
+    int o = y0 * nx;                                  // row offset (32-bit: the strip path needs nx*ny < 2^31)
+    float4 rm = ld4(uc, o - nx + i, act && y0 > 0);
+    float4 r0 = ld4(uc, o + i, act);
+    float sc0 = side ? uc[o + xs] : 0.f;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int j = y0 + r;
+        const bool okj = act && j < ny;
+        const bool okn = act && j + 1 < ny;
+        const float4 rp = ld4(uc, o + nx + i, okn);
+        const float scp = side && j + 1 < ny ? uc[o + nx + xs] : 0.f;
+        const float4 p = ld4(up, o + i, okj);
+        const float4 c = ld4(coef, o + i, okj);
+        const float4 d = ld4(dmap, o + i, okj);
+        float w = __shfl_up_sync(FULL, r0.w, 1), e = __shfl_down_sync(FULL, r0.x, 1);
+        if (lane == 0) w = sc0;
+        if (lane == 31) e = sc0;
+        float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
+        if (SRC && okj) {
+            const int4 rid = *reinterpret_cast<const int4*>(g.rid + o + i);
+            ax = rid.x >= 0 && rid.x / g.gs == ggl ? a : 0.f;
+            ay = rid.y >= 0 && rid.y / g.gs == ggl ? a : 0.f;
+            az = rid.z >= 0 && rid.z / g.gs == ggl ? a : 0.f;
+            aw = rid.w >= 0 && rid.w / g.gs == ggl ? a : 0.f;
+        }
+        float4 v;
+        v.x = fwd_cell(r0.y, w, rm.x, rp.x, r0.x, p.x, c.x, d.x, ax);
+        v.y = fwd_cell(r0.z, r0.x, rm.y, rp.y, r0.y, p.y, c.y, d.y, ay);
+        v.z = fwd_cell(r0.w, r0.y, rm.z, rp.z, r0.z, p.z, c.z, d.z, az);
+        v.w = fwd_cell(e, r0.z, rm.w, rp.w, r0.w, p.w, c.w, d.w, aw);
+        if (okj) {
+            *reinterpret_cast<float4*>(un + o + i) = v;
+            if (ck) *reinterpret_cast<float4*>(ck + o + i) = v;
+        }
+        rm = r0;
+        r0 = rp;
+        sc0 = scp;
+        o += nx;
+    }
+}
+
+template <int R>
+void fwdl_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    dim3 grid((g.nx + STRIP - 1) / STRIP, (g.ny + rows_per_block - 1) / rows_per_block + 1, s.ng);
+    if (s.k < g.n_src_steps) k_fwdl_strip<R, true><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+    else k_fwdl_strip<R, false><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+}
+
 template <int R, int D>
 void fwds_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
@@ -1466,6 +1559,10 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     case 5232: adj2s_strip<32, 2, 8>(g, coef, s, st); return;
     case 5316: adj2s_strip<16, 3, 8>(g, coef, s, st); return;
     case 5332: adj2s_strip<32, 3, 8>(g, coef, s, st); return;
+    case 7008: adjl2_strip<8, 4>(g, coef, s, st); return;   // 7000 + rows (+ 100: 3 blocks): lean
+    case 7016: adjl2_strip<16, 4>(g, coef, s, st); return;
+    case 7108: adjl2_strip<8, 3>(g, coef, s, st); return;
+    case 7116: adjl2_strip<16, 3>(g, coef, s, st); return;
     case 2004: adj2q_strip<4>(g, coef, s, st); return;     // 2000 + rows: four cells per lane
     case 2008: adj2q_strip<8>(g, coef, s, st); return;
     case 2016: adj2q_strip<16>(g, coef, s, st); return;
@@ -1478,7 +1575,10 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
 
 void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdStep& s, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
-    switch (rows) {   // 3000 + 100 D + rows: inputs staged in shared memory D rows ahead
+    switch (rows) {   // 3000 + 100 D + rows: inputs staged in shared memory D rows ahead; 6000 + rows: lean
+    case 6004: fwdl_strip<4>(g, coef, s, st); break;
+    case 6008: fwdl_strip<8>(g, coef, s, st); break;
+    case 6016: fwdl_strip<16>(g, coef, s, st); break;
     case 3204: fwds_strip<4, 2>(g, coef, s, st); break;
     case 3208: fwds_strip<8, 2>(g, coef, s, st); break;
     case 3216: fwds_strip<16, 2>(g, coef, s, st); break;
