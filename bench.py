@@ -361,9 +361,15 @@ def read_tuning(path):
         return None
     if not lines:
         return None
-    v = [int(x) for x in lines[-1][7:14]]
-    return {"fwd": f"two steps/launch, code {v[6]}" if v[5] else f"one step/launch, {v[0]} rows",
-            "adj": f"two steps/launch, {v[4]} rows" if v[3] else f"one step/launch, {v[1]} rows, variant {v[2]}"}
+    v = [int(x) for x in lines[-1][7:]] + [0] * 4
+    out = {"fwd": f"two steps/launch, code {v[6]}" if v[5] else f"one step/launch, code {v[0]}",
+           "adj": f"two steps/launch, code {v[4]}" if v[3] else f"one step/launch, {v[1]} rows, variant {v[2]}"}
+    if v[7]:
+        out["fwd"] = "tiles, 8 steps/launch"
+    if v[8]:
+        out["adj"] = "tiles, 6 steps/launch"
+    out["one_group_passes"] = {"fwd": "tiles" if v[9] else "as above", "adj": "tiles" if v[10] else "as above"}
+    return out
 
 
 def main():

@@ -140,3 +140,12 @@ __device__ __forceinline__ float damp_at(const DevGeo& g, int dcol, int drow) {
     const int dd = min(dcol, drow);
     return dd < g.sponge_w ? g.damp[dd] : 1.f;
 }
+
+// 16-byte asynchronous global-to-shared copy (cp.async, L2 only); ok == false zero-fills the
+// destination without reading the source.
+__device__ __forceinline__ void cp_async16(unsigned smem_addr, const float* gmem, bool ok) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr), "l"(gmem), "r"(ok ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }

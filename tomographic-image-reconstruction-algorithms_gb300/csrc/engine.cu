@@ -77,6 +77,8 @@ struct tomo_ctx {
     int rows_fwd2 = 8;
     bool tile_fwd = false;       // multi-step tile kernels (tile.cu) for the forward sweeps
     bool tile_adj = false;       // ... and for the adjoint sweeps
+    bool tile_fwd1 = false;      // the same choices for passes of one group (ART)
+    bool tile_adj1 = false;
     static constexpr int TILE_FWD_STEPS = 8;   // steps per forward tile launch
     // learned iteration (allocated on first use)
     float *illum = nullptr, *feat = nullptr, *fsave = nullptr, *dnet = nullptr, *dsave = nullptr;
@@ -250,14 +252,16 @@ bool tune_cache_read(tomo_ctx* c, const char* path) {
     bool hit = false;
     while (!hit && std::fgets(line, sizeof line, fp)) {
         if (std::strncmp(line, key.c_str(), key.size()) != 0 || line[key.size()] != ' ') continue;
-        int v[9] = {0};
-        const int nv = std::sscanf(line + key.size(), "%d %d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3],
-                                   &v[4], &v[5], &v[6], &v[7], &v[8]);
-        if (nv == 7 || nv == 9) {
+        int v[11] = {0};
+        const int nv = std::sscanf(line + key.size(), "%d %d %d %d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2],
+                                   &v[3], &v[4], &v[5], &v[6], &v[7], &v[8], &v[9], &v[10]);
+        if (nv == 7 || nv == 9 || nv == 11) {
             c->rows_fwd = v[0]; c->rows_adj = v[1]; c->adj_variant = v[2]; c->adj_pair = v[3] != 0;
             c->rows_adj2 = v[4]; c->fwd_pair = v[5] != 0 && c->S >= 4; c->rows_fwd2 = v[6];
             c->tile_fwd = v[7] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
             c->tile_adj = v[8] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
+            c->tile_fwd1 = v[9] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
+            c->tile_adj1 = v[10] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
             hit = true;
         }
     }
@@ -268,9 +272,9 @@ bool tune_cache_read(tomo_ctx* c, const char* path) {
 void tune_cache_append(const tomo_ctx* c, const char* path) {
     FILE* fp = std::fopen(path, "a");
     if (!fp) return;
-    std::fprintf(fp, "%s %d %d %d %d %d %d %d %d %d\n", tune_key(c).c_str(), c->rows_fwd, c->rows_adj,
+    std::fprintf(fp, "%s %d %d %d %d %d %d %d %d %d %d %d\n", tune_key(c).c_str(), c->rows_fwd, c->rows_adj,
                  c->adj_variant, c->adj_pair ? 1 : 0, c->rows_adj2, c->fwd_pair ? 1 : 0, c->rows_fwd2,
-                 c->tile_fwd ? 1 : 0, c->tile_adj ? 1 : 0);
+                 c->tile_fwd ? 1 : 0, c->tile_adj ? 1 : 0, c->tile_fwd1 ? 1 : 0, c->tile_adj1 ? 1 : 0);
     std::fclose(fp);
 }
 
@@ -280,8 +284,8 @@ void tile_override(tomo_ctx* c) {
     const char* e = std::getenv("TOMO_TILE");
     if (!e || !*e) return;
     const bool ok = tile_supported(c->dg, c->geo.cfg.profile);
-    c->tile_fwd = ok && (e[0] == '1' || e[0] == 'f');
-    c->tile_adj = ok && (e[0] == '1' || e[0] == 'a');
+    c->tile_fwd = c->tile_fwd1 = ok && (e[0] == '1' || e[0] == 'f');
+    c->tile_adj = c->tile_adj1 = ok && (e[0] == '1' || e[0] == 'a');
 }
 
 // Picks the strip kernels (rows per warp, register variant, one or two steps
@@ -426,6 +430,65 @@ tomo_status autotune(tomo_ctx* c) {
                          1e3 * ms_tf / reps, 1e3 * ms_ta / reps);
         c->tile_fwd = ms_tf < 0.97f * std::min(best_f1, c->fwd_pair ? best_f2 : best_f1);
         c->tile_adj = ms_ta < 0.97f * best_a;
+        c->tile_fwd1 = c->tile_fwd;
+        c->tile_adj1 = c->tile_adj;
+        if (c->geo.G > 1) {
+            // passes of one group (ART): the chosen strip kernels against the tiles, 8 steps each
+            float s_f = 1e30f, s_a = 1e30f, t_f = 1e30f, t_a = 1e30f;
+            for (int pass = 0; pass < passes; ++pass) {
+                float t_ms = 0.f;
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                for (int t = 0; t < reps;) {
+                    if (c->fwd_pair) {
+                        launch_fwd2_strip(c->rows_fwd2, c->dg, c->coef, fwd_args(c, k0 + t, 0, 1),
+                                          fwd_args(c, k0 + t + 1, 0, 1), false, false, c->st);
+                        t += 2;
+                    } else {
+                        launch_fwd_strip(c->rows_fwd, c->dg, c->coef, fwd_args(c, k0 + t, 0, 1), c->st);
+                        t += 1;
+                    }
+                }
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) s_f = std::min(s_f, t_ms);
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                for (int t = 0; t < reps;) {
+                    if (c->adj_pair) {
+                        launch_adj2_strip(c->rows_adj2, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, 1),
+                                          adj_args(c, k0 + reps - t - 1, 0, 1), c->st);
+                        t += 2;
+                    } else {
+                        launch_adj_strip(c->rows_adj, c->adj_variant, c->dg, c->coef, adj_args(c, k0 + reps - t, 0, 1),
+                                         c->st);
+                        t += 1;
+                    }
+                }
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) s_a = std::min(s_a, t_ms);
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, k0, reps, 0, 1), c->st);
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) t_f = std::min(t_f, t_ms);
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + reps + 1, 6, 0, 1), c->st);
+                launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + reps - 5, 2, 0, 1), c->st);
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) t_a = std::min(t_a, t_ms);
+            }
+            if (tlog)
+                std::fprintf(stderr, "tomo tune: one group: strip forward %.2f / tile %.2f us/step, strip adjoint "
+                             "%.2f / tile %.2f us/step\n", 1e3 * s_f / reps, 1e3 * t_f / reps, 1e3 * s_a / reps,
+                             1e3 * t_a / reps);
+            c->tile_fwd1 = t_f < 0.97f * s_f;
+            c->tile_adj1 = t_a < 0.97f * s_a;
+        }
     }
     tile_override(c);
     CU(c, cudaGetLastError());
@@ -560,6 +623,9 @@ tomo_status create_buffers(tomo_ctx* c) {
 // Kernel nodes the recorded pass contains (each launch_* call below is one kernel).
 int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     int64_t n = 0;
+    // multi-step tile kernels: the choice made for passes of one group when the pass has one
+    const bool tile_fwd = ng == 1 ? c->tile_fwd1 : c->tile_fwd;
+    const bool tile_adj = ng == 1 ? c->tile_adj1 : c->tile_adj;
     const Geometry& g = c->geo;
     const int nt = g.nt, S = c->S, K = c->K;
     const int64_t N = g.N, gstride = (int64_t)S * N, nch = g.nch, rpg = c->recs_per_group();
@@ -589,7 +655,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             fs.ckstride = (int64_t)c->nchunk * 2 * N;
         }
     };
-    if (c->tile_fwd) {
+    if (tile_fwd) {
         // multi-step tile launches: every slice 2 .. nt-1 is recorded by the launch computing it
         for (int k = 1; k <= nt - 2;) {
             const int T = std::min(tomo_ctx::TILE_FWD_STEPS, nt - 1 - k);
@@ -610,7 +676,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         }
     }
     int gnext = 2;   // strip path: slices 2 .. gnext-1 are recorded, in order
-    for (int k = 1; k <= nt - 2 && !c->tile_fwd;) {
+    for (int k = 1; k <= nt - 2 && !tile_fwd;) {
         FwdStep fs = fwd_args(c, k, g0, ng);
         const int m = k + 1;
         ck_of(fs, m);
@@ -651,7 +717,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         n += 2;
         k += 1;
     }
-    if (c->strip && !c->tile_fwd) {
+    if (c->strip && !tile_fwd) {
         for (int m = std::max(gnext, 2); m < nt - 1; ++m) {   // slices left before the last
             GatherStep gs{};
             gs.g0 = g0;
@@ -665,7 +731,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             ++n;
         }
     }
-    if (c->strip && !c->tile_fwd) {
+    if (c->strip && !tile_fwd) {
         GatherStep gs{};
         gs.g0 = g0;
         gs.u = c->hist + c->slot(nt - 1);
@@ -702,7 +768,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
                                        N, st);
                 }
                 for (int m = qa + 1; m <= qb;) {
-                    if (c->tile_fwd) {
+                    if (tile_fwd) {
                         const int T = std::min(tomo_ctx::TILE_FWD_STEPS, qb - m + 1);
                         launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, m - 1, T, g0, ng), st);
                         m += T;
@@ -719,7 +785,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             }
         }
         for (int q = qb; q >= qa;) {
-            if (c->tile_adj) {
+            if (tile_adj) {
                 const int T = tile_adj_steps(q - qa + 1);
                 launch_adj_tile(c->dg, c->coef, tile_adj_args(c, q + 1, T, g0, ng), st);
                 q -= T;

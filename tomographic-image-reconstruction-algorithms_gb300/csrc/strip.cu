@@ -591,12 +591,6 @@ void adj2q_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStre
 constexpr int ST_ARR = 6;                       // staged arrays per row
 constexpr int ST_ROW = ST_ARR * 64;             // floats per staged row
 
-__device__ __forceinline__ void cp_async16(unsigned smem_addr, const float* gmem, bool ok) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr), "l"(gmem), "r"(ok ? 16 : 0));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 // MB: minimum resident blocks per SM for the register allocator (7: 72 registers; 8: 64, one
 // wave of C2's 1152 blocks, at the price of a few spilled values).
