@@ -302,6 +302,7 @@ def time_to_image(ctx, w, sched, d_f, d_ft, torch, dev, plain_iters=30):
         return {"unavailable": "no trained weights at " + os.path.relpath(WEIGHTS, REPO)}
     net = tomo.Net(dev.index or 0)
     net.load(WEIGHTS)
+    ctx.set_learned_scale(tomo.LEARNED_SCALE)
     d_f.zero_()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -322,7 +323,8 @@ def time_to_image(ctx, w, sched, d_f, d_ft, torch, dev, plain_iters=30):
             "learned_seconds": t_learned, "learned_iters": len(leps),
             "learned_steps": "".join({1: "L", 0: "x", -1: "p"}[int(k)] for k in kind),
             "learned_epsilon": float(leps[-1]), "reached": reached,
-            "acceptance": {"min_decrease": tomo.LEARNED_MIN_DECREASE, "patience": tomo.LEARNED_PATIENCE},
+            "acceptance": {"min_decrease": tomo.LEARNED_MIN_DECREASE, "patience": tomo.LEARNED_PATIENCE,
+                           "scale": tomo.LEARNED_SCALE},
             "gradient_sweeps": {"plain": plain_iters, "learned": sweeps},
             "speedup": t_plain / t_learned if reached else None}
 

@@ -312,6 +312,10 @@ tomo_status tomo_run_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedule* 
                              int32_t patience, double* eps_log, int32_t* step_log, int32_t* iters_done,
                              int32_t* sweeps, double* seconds);
 
+/* Scale of the learned proposal: tomo_iterate_learned and tomo_run_learned propose
+ * f + scale * mask * net(features) (default 1; 0 < scale <= 4). */
+tomo_status tomo_set_learned_scale(tomo_ctx* ctx, double scale);
+
 /* Several independent reconstructions advanced together (the batched
  * many-phantom workload: phantoms of different grid sizes, each its own
  * context and stream).  Context i runs `iters` iterations of `method` from

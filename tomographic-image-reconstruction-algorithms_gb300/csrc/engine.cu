@@ -84,6 +84,7 @@ struct tomo_ctx {
     float *illum = nullptr, *feat = nullptr, *fsave = nullptr, *dnet = nullptr, *dsave = nullptr;
     unsigned int *illum_max = nullptr, *maxsave = nullptr;
     bool illum_ready = false;
+    double learned_scale = 1.0;  // the network's proposal is f + learned_scale * mask * net(features)
     static constexpr int ZR = 4; // adjoint ring slots
     bool tuned = false;
     std::vector<void*> allocs;
@@ -1487,7 +1488,7 @@ tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule
     if (ns != TOMO_OK) return c->fail(ns, "network: %s", tomo_net_last_error(net));
     c->launches += 6;
     CU(c, cudaMemcpyAsync(c->fsave, c->f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
-    launch_apply(c->f, c->dnet, c->mask, N, 1.0, nullptr, c->st);
+    launch_apply(c->f, c->dnet, c->mask, N, c->learned_scale, nullptr, c->st);
     launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
     c->launches += 2;
     TRY(next_noise_draw(c));
@@ -1553,7 +1554,7 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
             CU(c, cudaMemcpyAsync(c->fsave, c->f, fb, cudaMemcpyDeviceToDevice, c->st));
             CU(c, cudaMemcpyAsync(c->dsave, c->dir, fb, cudaMemcpyDeviceToDevice, c->st));
             CU(c, cudaMemcpyAsync(c->maxsave, c->maxabs, sizeof(unsigned int), cudaMemcpyDeviceToDevice, c->st));
-            launch_apply(c->f, c->dnet, c->mask, N, 1.0, nullptr, c->st);
+            launch_apply(c->f, c->dnet, c->mask, N, c->learned_scale, nullptr, c->st);
             c->launches += 7;
             // the check is the gradient sweep of the proposal: accepted, it is the next step's gradient
             TRY(features_core(c, &r1));
@@ -1698,6 +1699,13 @@ tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const
     return TOMO_OK;
 } catch (...) {
     return abi_exception(nullptr);
+}
+
+tomo_status tomo_set_learned_scale(tomo_ctx* c, double scale) {
+    if (!c) return TOMO_ERR_ARG;
+    if (!(scale > 0.0 && scale <= 4.0)) return c->fail(TOMO_ERR_ARG, "learned scale must be in (0, 4]");
+    c->learned_scale = scale;
+    return TOMO_OK;
 }
 
 tomo_status tomo_synchronize(tomo_ctx* c) try {

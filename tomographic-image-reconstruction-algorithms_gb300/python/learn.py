@@ -38,6 +38,7 @@ sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 import tomo  # noqa: E402
 
 STEP = 0.02          # plain weighted SIRT step (direction scaled to max 1 over the mask)
+LEARNED_SCALE = tomo.LEARNED_SCALE   # the proposal is f + LEARNED_SCALE * mask * net(features)
 WEIGHTS = os.path.join(tomo.PKG_DIR, "weights", "learned_update.bin")
 
 
@@ -244,17 +245,20 @@ def time_to_image(net, plain_iters=30, seed=2001, device=0,
         out = {"plain_iters": plain_iters, "plain_seconds": t_plain, "plain_final_epsilon": target,
                "plain_epsilon": eps, "learned": {}}
         for rule in rules:
+            md, pat = rule[0], rule[1]
+            scale = rule[2] if len(rule) > 2 else LEARNED_SCALE
+            ctx.set_learned_scale(scale)
             d_f.zero_()
             torch.cuda.synchronize(dev)
             leps, kind, sweeps, t_learned = ctx.run_learned(net, sched, d_f.data_ptr(), d_fo.data_ptr(), target,
-                                                            3 * plain_iters, *rule)
+                                                            3 * plain_iters, md, pat)
             leps = [float(e) for e in leps]
             reached = bool(leps[-1] <= target)
             steps = "".join({1: "L", 0: "x", -1: "p"}[int(k)] for k in kind)
-            log(f"  learned (min decrease {rule[0]}, patience {rule[1]}): {steps}, {sweeps} sweeps, "
+            log(f"  learned (min decrease {md}, patience {pat}, scale {scale}): {steps}, {sweeps} sweeps, "
                 f"eps -> {leps[-1]:.3f} %, {t_learned:.3f} s, speedup "
                 f"{t_plain / t_learned if reached else float('nan'):.2f}")
-            out["learned"]["%g/%d" % rule] = {
+            out["learned"]["%g/%d/%g" % (md, pat, scale)] = {
                 "iters": len(leps), "steps": steps, "sweeps": sweeps, "seconds": t_learned,
                 "final_epsilon": leps[-1], "epsilon": leps, "reached": reached,
                 "speedup": t_plain / t_learned if reached else None}
@@ -275,6 +279,8 @@ def main():
     ap.add_argument("--onpolicy-iters", type=int, default=20)
     ap.add_argument("--eval-only", action="store_true")
     ap.add_argument("--eval-seeds", default="2001", help="comma-separated phantom seeds of the evaluation")
+    ap.add_argument("--eval-scales", default="", help="comma-separated learned-step scales to evaluate "
+                                                         "(default: the shipped one)")
     args = ap.parse_args()
     import torch
 
@@ -321,7 +327,9 @@ def main():
     report["time_to_image"] = {}
     for seed in [int(x) for x in args.eval_seeds.split(",")]:
         print(f"  evaluation phantom seed {seed}")
-        report["time_to_image"][str(seed)] = time_to_image(net, seed=seed)
+        rules = tuple((tomo.LEARNED_MIN_DECREASE, tomo.LEARNED_PATIENCE, float(x))
+                      for x in (args.eval_scales.split(",") if args.eval_scales else [LEARNED_SCALE]))
+        report["time_to_image"][str(seed)] = time_to_image(net, seed=seed, rules=rules)
     print(json.dumps(report))
 
 

@@ -37,6 +37,8 @@ SCHED_CONST, SCHED_POWER, SCHED_LINEAR = range(3)
 # acceptance rule of the learned step (tomo_run_learned): a proposal must lower the squared
 # record residual by 5 %; after 2 rejections in a row the run continues with plain steps
 LEARNED_MIN_DECREASE, LEARNED_PATIENCE = 0.05, 2
+# scale of the learned proposal f + LEARNED_SCALE * mask * net(features) (tomo_set_learned_scale)
+LEARNED_SCALE = 1.0
 
 
 class Config(C.Structure):
@@ -180,6 +182,7 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_net_grad_device": (i32, [vp, vp, vp, vp, i32, i32, i32, FP, DP]),
         "tomo_net_train_step_device": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, DP]),
         "tomo_features_device": (i32, [vp, vp, vp, DP]),
+        "tomo_set_learned_scale": (i32, [vp, C.c_double]),
         "tomo_iterate_learned": (i32, [vp, vp, C.POINTER(Schedule), i32, vp, vp, C.POINTER(IterStats), IP]),
         "tomo_run_learned": (i32, [vp, vp, C.POINTER(Schedule), vp, vp, C.c_double, i32, C.c_double, i32, DP, IP,
                                    IP, IP, C.POINTER(C.c_double)]),
@@ -386,6 +389,10 @@ class Context:
                                            C.byref(secs)))
         n = done.value
         return eps[:n], kind[:n], sweeps.value, secs.value
+
+    def set_learned_scale(self, scale: float):
+        """Scale of the learned proposal f + scale * mask * net(features)."""
+        self._check(lib().tomo_set_learned_scale(self.h, scale))
 
     @property
     def stream(self) -> int:
