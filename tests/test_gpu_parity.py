@@ -306,7 +306,8 @@ def test_errors_are_status_codes():
 
 
 @pytest.mark.parametrize("adj_rows", ["1004", "1108", "1216", "232", "2008", "2032", "4008", "4132",
-                                      "3204", "3308", "3332", "3416", "5232", "5316", "7008", "7016", "7108"])
+                                      "3204", "3308", "3332", "3416", "5232", "5316", "7008", "7016", "7108",
+                                      "8208", "8308", "8408", "8316"])
 def test_two_step_adjoint_variants_match_one_step(adj_rows, monkeypatch):
     """The two-step adjoint's variants (interior fast path, inputs read ahead, four cells per
     lane, packed FP32x2 arithmetic, inputs staged in shared memory by cp.async) give the
@@ -328,7 +329,7 @@ def test_two_step_adjoint_variants_match_one_step(adj_rows, monkeypatch):
     assert outs[0][1] == outs[1][1]
 
 
-@pytest.mark.parametrize("rows", ["3204", "3308", "3316", "6004", "6008", "6016"])
+@pytest.mark.parametrize("rows", ["3204", "3308", "3316", "6004", "6008", "6016", "6104", "6116"])
 def test_staged_one_step_forward_matches(rows, monkeypatch):
     """The one-step forward with staged inputs, and the lean form with the sponge map, give the
     register kernel's records and gradients bit for bit (nx 256: interior strips; ny 96: with

@@ -365,9 +365,10 @@ tomo_status autotune(tomo_ctx* c) {
         // two steps per launch (reps/2 launches cover the same steps); codes as launch_adj2_strip
         for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows, 2000 + rows,
                          4000 + rows, 4100 + rows, 3200 + rows, 3300 + rows, 3400 + rows, 5200 + rows,
-                         5300 + rows, 7000 + rows, 7100 + rows}) {
+                         5300 + rows, 7000 + rows, 7100 + rows, 8200 + rows, 8300 + rows, 8400 + rows}) {
             if (code >= 5000 && code < 7000 && rows < 16) continue;   // 8-block staged build: rows 16, 32
-            if (code >= 7000 && rows != 8 && rows != 16) continue;    // lean build: rows 8, 16
+            if (code >= 7000 && code < 8000 && rows != 8 && rows != 16) continue;   // lean build: rows 8, 16
+            if (code >= 8000 && rows != 8 && code != 8316) continue;  // unrolled staged build: rows 8 (16 at D 3)
             if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {
@@ -386,7 +387,7 @@ tomo_status autotune(tomo_ctx* c) {
         }
     }
     // one-step forward with its inputs staged in shared memory
-    for (int code : {3204, 3208, 3216, 3304, 3308, 3316, 6004, 6008, 6016}) {
+    for (int code : {3204, 3208, 3216, 3304, 3308, 3316, 6004, 6008, 6016, 6104, 6108, 6116}) {
         if (code % 100 > 4 * c->geo.ny) continue;
         float ms = 1e30f;
         for (int pass = 0; pass < passes; ++pass) {

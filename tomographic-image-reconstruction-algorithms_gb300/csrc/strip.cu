@@ -594,7 +594,8 @@ constexpr int ST_ROW = ST_ARR * 64;             // floats per staged row
 
 // MB: minimum resident blocks per SM for the register allocator (7: 72 registers; 8: 64, one
 // wave of C2's 1152 blocks, at the price of a few spilled values).
-template <int R, int D, int MB = 7>
+// UNR: the row loop fully unrolled (ring slots and the receiver-bit shift become constants).
+template <int R, int D, int MB = 7, bool UNR = false>
 __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
     extern __shared__ float4 st_mem4[];
     const int nx = g.nx, ny = g.ny;
@@ -665,9 +666,12 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
         if (y0 - 1 + t <= rlast) stage(y0 - 1 + t, t);
         cp_async_commit();
     }
-    int slot = 0;                                        // slot of row r
-#pragma unroll 1
-    for (int r = y0 - 1; r <= rlast; ++r) {
+    constexpr int UNROLL = UNR ? R + 2 : 1;
+#pragma unroll UNROLL
+    for (int t = 0; t < R + 2; ++t) {
+        const int r = y0 - 1 + t;
+        if (r > rlast) break;
+        const int slot = t % D;                          // slot of row r
         const int row = r * nx;
         const bool ok = row_ok(r);
         cp_async_wait<D - 1>();                          // this lane's copies of row r are done
@@ -682,8 +686,7 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
         __syncwarp();                                    // the slot is free for row r+D
         if (r + D <= rlast) stage(r + D, slot);
         cp_async_commit();
-        slot = slot + 1 == D ? 0 : slot + 1;
-        const bool rcv = (rbits >> (r - y0 + 1)) & 1ull;
+        const bool rcv = (rbits >> t) & 1ull;
         int2 rid = make_int2(-1, -1);
         if (rcv && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
         const float2 pzp = mul2(cp, z1p);
@@ -758,12 +761,12 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
     cp_async_wait<0>();                                  // nothing left in flight at exit
 }
 
-template <int R, int D, int MB = 7>
+template <int R, int D, int MB = 7, bool UNR = false>
 void adj2s_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     const size_t smem = sizeof(float) * WARPS * D * ST_ROW;
     dim3 grid((g.nx + 2 + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
-    k_adj2s_strip<R, D, MB><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
+    k_adj2s_strip<R, D, MB, UNR><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1361,8 +1364,8 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_fwds_strip(DevGeo g, const fl
 // term only in launches of source steps (SRC), the west / east neighbours of a lane's four cells
 // by shuffles with one predicated scalar load at each strip end.  Same cell arithmetic
 // (fwd_cell) as every other forward kernel, so the same bits.
-template <int R, bool SRC>
-__global__ void __launch_bounds__(WARPS * 32, 8) k_fwdl_strip(DevGeo g, const float* __restrict__ coef, FwdStep s) {
+template <int R, bool SRC, bool PF>
+__global__ void __launch_bounds__(WARPS * 32, PF ? 7 : 8) k_fwdl_strip(DevGeo g, const float* __restrict__ coef, FwdStep s) {
     const int nx = g.nx, ny = g.ny;
     const int gl = blockIdx.z;
     if (blockIdx.y == gridDim.y - 1) {
@@ -1400,16 +1403,40 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_fwdl_strip(DevGeo g, const fl
     float4 rm = ld4(uc, o - nx + i, act && y0 > 0);
     float4 r0 = ld4(uc, o + i, act);
     float sc0 = side ? uc[o + xs] : 0.f;
+    // PF: the inputs of row r+1 are requested before row r is computed (two rows of loads in flight)
+    float4 q_rp, q_p, q_c, q_d;
+    float q_sc = 0.f;
+    if (PF) {
+        q_rp = ld4(uc, o + nx + i, act && y0 + 1 < ny);
+        q_sc = side && y0 + 1 < ny ? uc[o + nx + xs] : 0.f;
+        q_p = ld4(up, o + i, act);
+        q_c = ld4(coef, o + i, act);
+        q_d = ld4(dmap, o + i, act);
+    }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int j = y0 + r;
         const bool okj = act && j < ny;
-        const bool okn = act && j + 1 < ny;
-        const float4 rp = ld4(uc, o + nx + i, okn);
-        const float scp = side && j + 1 < ny ? uc[o + nx + xs] : 0.f;
-        const float4 p = ld4(up, o + i, okj);
-        const float4 c = ld4(coef, o + i, okj);
-        const float4 d = ld4(dmap, o + i, okj);
+        float4 rp, p, c, d;
+        float scp;
+        if (PF) {
+            rp = q_rp; p = q_p; c = q_c; d = q_d; scp = q_sc;
+            if (r + 1 < R) {
+                const bool ok1 = act && j + 1 < ny, ok2 = act && j + 2 < ny;
+                q_rp = ld4(uc, o + 2 * nx + i, ok2);
+                q_sc = side && j + 2 < ny ? uc[o + 2 * nx + xs] : 0.f;
+                q_p = ld4(up, o + nx + i, ok1);
+                q_c = ld4(coef, o + nx + i, ok1);
+                q_d = ld4(dmap, o + nx + i, ok1);
+            }
+        } else {
+            const bool okn = act && j + 1 < ny;
+            rp = ld4(uc, o + nx + i, okn);
+            scp = side && j + 1 < ny ? uc[o + nx + xs] : 0.f;
+            p = ld4(up, o + i, okj);
+            c = ld4(coef, o + i, okj);
+            d = ld4(dmap, o + i, okj);
+        }
         float w = __shfl_up_sync(FULL, r0.w, 1), e = __shfl_down_sync(FULL, r0.x, 1);
         if (lane == 0) w = sc0;
         if (lane == 31) e = sc0;
@@ -1437,12 +1464,12 @@ __global__ void __launch_bounds__(WARPS * 32, 8) k_fwdl_strip(DevGeo g, const fl
     }
 }
 
-template <int R>
+template <int R, bool PF = false>
 void fwdl_strip(const DevGeo& g, const float* coef, const FwdStep& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     dim3 grid((g.nx + STRIP - 1) / STRIP, (g.ny + rows_per_block - 1) / rows_per_block + 1, s.ng);
-    if (s.k < g.n_src_steps) k_fwdl_strip<R, true><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
-    else k_fwdl_strip<R, false><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+    if (s.k < g.n_src_steps) k_fwdl_strip<R, true, PF><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
+    else k_fwdl_strip<R, false, PF><<<grid, WARPS * 32, 0, st>>>(g, coef, s);
 }
 
 template <int R, int D>
@@ -1549,6 +1576,10 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     case 3408: adj2s_strip<8, 4>(g, coef, s, st); return;
     case 3416: adj2s_strip<16, 4>(g, coef, s, st); return;
     case 3432: adj2s_strip<32, 4>(g, coef, s, st); return;
+    case 8208: adj2s_strip<8, 2, 6, true>(g, coef, s, st); return;    // 8000 + 100 D + rows: staged, unrolled
+    case 8308: adj2s_strip<8, 3, 6, true>(g, coef, s, st); return;
+    case 8408: adj2s_strip<8, 4, 6, true>(g, coef, s, st); return;
+    case 8316: adj2s_strip<16, 3, 6, true>(g, coef, s, st); return;
     case 5216: adj2s_strip<16, 2, 8>(g, coef, s, st); return;   // 5000 + 100 D + rows: staged, 8 blocks
     case 5232: adj2s_strip<32, 2, 8>(g, coef, s, st); return;
     case 5316: adj2s_strip<16, 3, 8>(g, coef, s, st); return;
@@ -1573,6 +1604,9 @@ void launch_fwd_strip(int rows, const DevGeo& g, const float* coef, const FwdSte
     case 6004: fwdl_strip<4>(g, coef, s, st); break;
     case 6008: fwdl_strip<8>(g, coef, s, st); break;
     case 6016: fwdl_strip<16>(g, coef, s, st); break;
+    case 6104: fwdl_strip<4, true>(g, coef, s, st); break;   // 6100 + rows: lean, next row requested ahead
+    case 6108: fwdl_strip<8, true>(g, coef, s, st); break;
+    case 6116: fwdl_strip<16, true>(g, coef, s, st); break;
     case 3204: fwds_strip<4, 2>(g, coef, s, st); break;
     case 3208: fwds_strip<8, 2>(g, coef, s, st); break;
     case 3216: fwds_strip<16, 2>(g, coef, s, st); break;
