@@ -512,13 +512,16 @@ def main():
     dom = ("forward_step", fwd_ms, fwd_b) if share_f >= share_a else ("adjoint_step", adj_ms, adj_b)
     peak, peak_kind = peaks()
     achieved = dom[2] / (dom[1] * 1e-3) / 1e9
-    traffic = None
+    traffic, tr_all = None, {}
     tpath = os.path.join(REPO, "profiles", f"traffic_{args.workload}.json")
-    if os.path.exists(tpath):
+    if os.path.exists(tpath) and args.nt <= 0:
         try:
-            traffic = json.load(open(tpath)).get(dom[0])
+            tr_all = json.load(open(tpath))
+            traffic = tr_all.get(dom[0])
         except Exception:
-            traffic = None
+            traffic, tr_all = None, {}
+    # the sweep's time accounted by the per-step kernel times (graph-replayed, as in the iteration)
+    sweep_ms = fwd_launches * fwd_ms + adj_launches * adj_ms
 
     if rank == 0:
         line = {
@@ -540,7 +543,12 @@ def main():
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "ms_per_launch": dom[1], "bytes_per_launch": dom[2],
                          "other": {"forward_step_GBps": fwd_b / (fwd_ms * 1e-3) / 1e9,
-                                   "adjoint_step_GBps": adj_b / (adj_ms * 1e-3) / 1e9}},
+                                   "adjoint_step_GBps": adj_b / (adj_ms * 1e-3) / 1e9,
+                                   "forward_step_ms": fwd_ms, "adjoint_step_ms": adj_ms,
+                                   "forward_steps": fwd_launches, "adjoint_steps": adj_launches,
+                                   "steps_ms": sweep_ms,
+                                   "algorithmic_bytes": {"forward_step": fwd_b, "adjoint_step": adj_b},
+                                   "dram_bytes": {k: tr_all.get(k) for k in ("forward_step", "adjoint_step")}}},
             "clocks": clocks,
         }
         if tti is not None:

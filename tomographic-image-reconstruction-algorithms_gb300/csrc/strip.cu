@@ -770,6 +770,171 @@ void adj2s_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStre
 }
 
 // ---------------------------------------------------------------------------
+// Two adjoint steps per launch, staged, four cells per lane: 128-cell strips overlapping by one
+// lane (4 cells) on each side (lanes 1..30 write 120 cells), the row inputs in a per-warp
+// shared-memory ring of D rows filled by cp.async (each lane copies one 16-byte chunk of each
+// of the six arrays per row), the sponge factor from the per-cell map (read one row ahead), the
+// row loop fully unrolled.  Rolling state and cell arithmetic are those of k_adj2_strip, so the
+// results are identical.
+constexpr int S4_ROW = ST_ARR * 128;           // floats per staged row (six arrays of 128 cells)
+
+template <int R, int D, int MB>
+__global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s4_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
+    extern __shared__ float4 st_mem4[];
+    const int nx = g.nx, ny = g.ny;
+    const int gl = blockIdx.z;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 120 - 4;
+    const int i = x0 + 4 * lane;
+    const int y0 = (blockIdx.y * WARPS + warp) * R;
+    if (y0 >= ny) return;
+    float* ring = reinterpret_cast<float*>(st_mem4) + warp * D * S4_ROW;
+    const bool in = i >= 0 && i < nx;                // nx % 4 == 0: a lane's chunk is all in or out
+    const bool own = in && lane >= 1 && lane <= 30;
+    const float* z1 = s.z1 + gl * s.zstride;
+    const float* z2 = s.z2 + gl * s.zstride;
+    float* za = s.za + gl * s.zstride;
+    float* zb = s.zb + gl * s.zstride;
+    const float* ua = s.ua + gl * s.ustride;
+    const float* ub = s.ub + gl * s.ustride;
+    const float* rra = s.rra + gl * s.rrstride;
+    const float* rrb = s.rrb + gl * s.rrstride;
+    float* corr = s.corr + gl * s.cstride;
+    const float* dmap = g.dmap;
+    auto row_ok = [&](int r) { return in && r >= 0 && r < ny; };
+    const RcvMask rk = rcv_mask(g, x0, x0 + 128);
+    const unsigned rb_lo = __ballot_sync(FULL, rcv_row(g, rk, y0 - 1 + lane));
+    const unsigned rb_hi = R + 2 > 32 ? __ballot_sync(FULL, rcv_row(g, rk, y0 + 31 + lane)) : 0u;
+    const unsigned long long rbits = ((unsigned long long)rb_hi << 32) | rb_lo;
+    // staged arrays: 0 z1(t+1), 1 coef(t+1), 2 z2(t), 3 ua(t), 4 ub(t), 5 corr(t); lane copies its chunk
+    const unsigned ring_s = (unsigned)__cvta_generic_to_shared(ring) + 16u * (unsigned)lane;
+    auto stage = [&](int t, int slot) {                 // row t of the schedule into `slot`
+        const unsigned dst = ring_s + 4u * (unsigned)(slot * S4_ROW);
+        const bool r1 = row_ok(t + 1), r0 = row_ok(t);
+        const int o0 = t * nx + i;
+        cp_async16(dst + 4u * 0 * 128, z1 + (r1 ? o0 + nx : 0), r1);
+        cp_async16(dst + 4u * 1 * 128, coef + (r1 ? o0 + nx : 0), r1);
+        cp_async16(dst + 4u * 2 * 128, z2 + (r0 ? o0 : 0), r0);
+        cp_async16(dst + 4u * 3 * 128, ua + (r0 ? o0 : 0), r0);
+        cp_async16(dst + 4u * 4 * 128, ub + (r0 ? o0 : 0), r0);
+        cp_async16(dst + 4u * 5 * 128, corr + (r0 ? o0 : 0), r0);
+    };
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    int o = (y0 - 1) * nx;
+    float4 z1m = ld4(z1, o - nx + i, row_ok(y0 - 2));
+    float4 z10 = ld4(z1, o + i, row_ok(y0 - 1));
+    float4 pzm = mul4(ld4(coef, o - nx + i, row_ok(y0 - 2)), z1m);
+    float4 c0 = ld4(coef, o + i, row_ok(y0 - 1));
+    float4 pz0 = mul4(c0, z10);
+    float4 zam = zero, pam2 = zero, pam = zero, uam2 = zero, uam = zero, ubm2 = zero, ubm = zero, crm = zero;
+    float4 dm = zero;
+    float4 d0 = ld4(dmap, o + i, row_ok(y0 - 1));       // sponge of row r, read one row ahead
+    int4 ridm = make_int4(-1, -1, -1, -1);
+    bool rcvm = false;
+    const int rlast = min(y0 + R, ny);
+#pragma unroll
+    for (int t = 0; t < D; ++t) {                        // prologue: rows y0-1 .. y0+D-2
+        if (y0 - 1 + t <= rlast) stage(y0 - 1 + t, t);
+        cp_async_commit();
+    }
+#pragma unroll
+    for (int t = 0; t < R + 2; ++t) {
+        const int r = y0 - 1 + t;
+        if (r > rlast) break;
+        const int slot = t % D;
+        const bool ok = row_ok(r);
+        cp_async_wait<D - 1>();
+        __syncwarp();
+        const float* sr = ring + slot * S4_ROW + 4 * lane;
+        const float4 z1p = *reinterpret_cast<const float4*>(sr + 0 * 128);
+        const float4 cp = *reinterpret_cast<const float4*>(sr + 1 * 128);
+        const float4 zz = *reinterpret_cast<const float4*>(sr + 2 * 128);
+        const float4 ua0 = *reinterpret_cast<const float4*>(sr + 3 * 128);
+        const float4 ub0 = *reinterpret_cast<const float4*>(sr + 4 * 128);
+        const float4 cr_next = *reinterpret_cast<const float4*>(sr + 5 * 128);
+        __syncwarp();
+        if (r + D <= rlast) stage(r + D, slot);
+        cp_async_commit();
+        const float4 d1 = ld4(dmap, o + nx + i, row_ok(r + 1));   // next row's sponge
+        const bool rcv = (rbits >> t) & 1ull;
+        int4 rid = make_int4(-1, -1, -1, -1);
+        if (rcv && ok) rid = *reinterpret_cast<const int4*>(g.rid + o + i);
+        const float4 pzp = mul4(cp, z1p);
+        float4 za0 = zero;
+        {
+            const float pw = __shfl_up_sync(FULL, pz0.w, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
+            if (ok) {
+                float4 inj = zero;
+                if (rcv) {
+                    inj.x = rid.x >= 0 ? rra[rid.x] : 0.f;
+                    inj.y = rid.y >= 0 ? rra[rid.y] : 0.f;
+                    inj.z = rid.z >= 0 ? rra[rid.z] : 0.f;
+                    inj.w = rid.w >= 0 ? rra[rid.w] : 0.f;
+                }
+                za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, inj.x, d0.x);
+                za0.y = adj_cell(pz0.z, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, inj.y, d0.y);
+                za0.z = adj_cell(pz0.w, pz0.y, pzm.z, pzp.z, pz0.z, z10.z, zz.z, inj.z, d0.z);
+                za0.w = adj_cell(pe, pz0.z, pzm.w, pzp.w, pz0.w, z10.w, zz.w, inj.w, d0.w);
+            }
+        }
+        const float4 pa0 = mul4(c0, za0);
+        {
+            const float pw = __shfl_up_sync(FULL, pam.w, 1), pe = __shfl_down_sync(FULL, pam.x, 1);
+            const float uaw = __shfl_up_sync(FULL, uam.w, 1), uae = __shfl_down_sync(FULL, uam.x, 1);
+            const float ubw = __shfl_up_sync(FULL, ubm.w, 1), ube = __shfl_down_sync(FULL, ubm.x, 1);
+            if (t >= 2 && own && r - 1 < ny) {
+                const int ob = o - nx;
+                float4 inj = zero;
+                if (rcvm) {
+                    inj.x = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
+                    inj.y = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
+                    inj.z = ridm.z >= 0 ? rrb[ridm.z] : 0.f;
+                    inj.w = ridm.w >= 0 ? rrb[ridm.w] : 0.f;
+                }
+                float4 zbv;
+                zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, inj.x, dm.x);
+                zbv.y = adj_cell(pam.z, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, inj.y, dm.y);
+                zbv.z = adj_cell(pam.w, pam.y, pam2.z, pa0.z, pam.z, zam.z, z1m.z, inj.z, dm.z);
+                zbv.w = adj_cell(pe, pam.z, pam2.w, pa0.w, pam.w, zam.w, z1m.w, inj.w, dm.w);
+                float4 cr = crm;
+                cr.x = __fmaf_rn(zam.x, lap5(uam.y, uaw, uam2.x, ua0.x, uam.x), cr.x);
+                cr.y = __fmaf_rn(zam.y, lap5(uam.z, uam.x, uam2.y, ua0.y, uam.y), cr.y);
+                cr.z = __fmaf_rn(zam.z, lap5(uam.w, uam.y, uam2.z, ua0.z, uam.z), cr.z);
+                cr.w = __fmaf_rn(zam.w, lap5(uae, uam.z, uam2.w, ua0.w, uam.w), cr.w);
+                cr.x = __fmaf_rn(zbv.x, lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x), cr.x);
+                cr.y = __fmaf_rn(zbv.y, lap5(ubm.z, ubm.x, ubm2.y, ub0.y, ubm.y), cr.y);
+                cr.z = __fmaf_rn(zbv.z, lap5(ubm.w, ubm.y, ubm2.z, ub0.z, ubm.z), cr.z);
+                cr.w = __fmaf_rn(zbv.w, lap5(ube, ubm.z, ubm2.w, ub0.w, ubm.w), cr.w);
+                *reinterpret_cast<float4*>(corr + ob + i) = cr;
+                *reinterpret_cast<float4*>(za + ob + i) = zam;
+                *reinterpret_cast<float4*>(zb + ob + i) = zbv;
+            }
+        }
+        z1m = z10; z10 = z1p;
+        pzm = pz0; pz0 = pzp;
+        c0 = cp;
+        zam = za0;
+        pam2 = pam; pam = pa0;
+        uam2 = uam; uam = ua0;
+        ubm2 = ubm; ubm = ub0;
+        dm = d0; d0 = d1;
+        ridm = rid;
+        rcvm = rcv;
+        crm = cr_next;
+        o += nx;
+    }
+    cp_async_wait<0>();
+}
+
+template <int R, int D, int MB>
+void adj2s4_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
+    const int rows_per_block = WARPS * R;
+    const size_t smem = sizeof(float) * WARPS * D * S4_ROW;
+    dim3 grid((g.nx + 119) / 120, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
+    k_adj2s4_strip<R, D, MB><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
+}
+
+// ---------------------------------------------------------------------------
 // Two adjoint steps per launch, lean form: four cells per lane, 128-cell strips overlapping by
 // one lane (4 cells) on each side (lanes 1..30, 120 cells, write; lanes 0 and 31 compute the
 // first step as halo), rows y0-1 .. y0+R in a fully unrolled loop with every access predicated,
@@ -1576,6 +1741,10 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     case 3408: adj2s_strip<8, 4>(g, coef, s, st); return;
     case 3416: adj2s_strip<16, 4>(g, coef, s, st); return;
     case 3432: adj2s_strip<32, 4>(g, coef, s, st); return;
+    case 9208: adj2s4_strip<8, 2, 4>(g, coef, s, st); return;   // 9000 + 100 D + rows: staged, 4 cells/lane
+    case 9308: adj2s4_strip<8, 3, 4>(g, coef, s, st); return;
+    case 9216: adj2s4_strip<16, 2, 3>(g, coef, s, st); return;
+    case 9316: adj2s4_strip<16, 3, 3>(g, coef, s, st); return;
     case 8208: adj2s_strip<8, 2, 6, true>(g, coef, s, st); return;    // 8000 + 100 D + rows: staged, unrolled
     case 8308: adj2s_strip<8, 3, 6, true>(g, coef, s, st); return;
     case 8408: adj2s_strip<8, 4, 6, true>(g, coef, s, st); return;
