@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -69,16 +70,51 @@ WORKLOADS = {
 C3_SIZES = (128, 192, 256, 384, 512)
 
 
-def c3_configs(device, n=64):
+def c3_configs(device, n=64, timed_plans=False, memory=None):
     """The batched workload: n phantoms cycling through the grid sizes N, N/2 transducers on a
-    radius-0.43N circle in groups of 8, nt = 10 N, checkpoint interval about sqrt(2 nt)."""
+    radius-0.43N circle in groups of 8, nt = 10 N.  Checkpoint interval: about sqrt(2 nt), or
+    with timed_plans the library's timed choice (ckpt_interval -1) under a per-phantom memory cap
+    (c3_memory_caps over `memory` bytes)."""
     out = []
     for i in range(n):
         N = C3_SIZES[i % len(C3_SIZES)]
         nt = 10 * N
         out.append(tomo.cfg_config(nx=N, ny=N, nt=nt, n_transducers=N // 2, group_size=8, radius=0.43 * N,
-                                   ckpt_interval=int(round((2 * nt) ** 0.5)), device=device))
+                                   ckpt_interval=-1 if timed_plans else int(round((2 * nt) ** 0.5)), device=device))
+    if timed_plans:
+        for cfg, cap in zip(out, c3_memory_caps(out, memory)):
+            cfg.mem_limit_mb = int(cap // (1 << 20))
     return out
+
+
+def plan_bytes(cfg, full, K=0):
+    """Device bytes of a context under a memory plan with all groups resident: the plan's
+    per-group buffers (forward slots, adjoint ring of 4, checkpoints, residual records) and the
+    fixed ones, as the library's plan counts them (plus 64 MiB of slack)."""
+    G, N, nt, nch = tomo.n_groups(cfg), cfg.nx * cfg.ny, cfg.nt, tomo.n_channels(cfg)
+    slots = nt if full else K + 1
+    chunks = 0 if full else -(-(nt - 2) // K)
+    per_group = 4 * ((slots + 4 + 2 * chunks) * N + nt * nch)
+    fixed = 4 * 7 * N + 4 * 2 * G * N + 4 * 2 * G * nt * nch + 8 * G * nt + 8 * (G + 2) * 1024 + (64 << 20)
+    return G * per_group + fixed
+
+
+def c3_memory_caps(cfgs, memory):
+    """Memory caps of the batch: every phantom gets its least-memory plan (K = ceil(sqrt(2 (nt-2))));
+    what is left goes, smallest first, to phantoms whose full forward history then fits; the rest
+    is shared in proportion to the caps.  The library times its plans inside each cap."""
+    ks = [max(4, math.ceil(math.sqrt(2.0 * (c.nt - 2)))) for c in cfgs]
+    caps = [plan_bytes(c, False, k) for c, k in zip(cfgs, ks)]
+    left = memory - sum(caps)
+    if left < 0:
+        raise RuntimeError(f"the batch needs {sum(caps) / 1e9:.1f} GB at least, {memory / 1e9:.1f} GB available")
+    for i in sorted(range(len(cfgs)), key=lambda i: plan_bytes(cfgs[i], True)):
+        extra = plan_bytes(cfgs[i], True) - caps[i]
+        if 0 < extra <= left:
+            caps[i] += extra
+            left -= extra
+    tot = sum(caps)
+    return [c + left * c / tot for c in caps]
 
 
 def run_batch(args, local, rank, world, dist):
@@ -86,7 +122,11 @@ def run_batch(args, local, rank, world, dist):
     import torch
 
     dev = torch.device("cuda", local)
-    cfgs = c3_configs(local)
+    # plan and kernel choices are timed once per grid size and reused through the tuning cache
+    if not os.environ.get("TOMO_TUNE_CACHE"):
+        os.environ["TOMO_TUNE_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="tomo_tune_"), "tune.txt")
+    free_b, _ = torch.cuda.mem_get_info(dev)
+    cfgs = c3_configs(local, timed_plans=True, memory=0.85 * free_b)
     ctxs, d_fs, d_fts, recs, fos = [], [], [], [], []
     for i, cfg in enumerate(cfgs):
         N = cfg.nx
@@ -102,6 +142,13 @@ def run_batch(args, local, rank, world, dist):
     torch.cuda.synchronize(dev)
     sched = tomo.schedule(omega=0.02, normalize=1)
     bytes_it = sum(algorithmic_bytes(c, tomo.n_groups(c)) for c in cfgs)
+    # the timed memory plan each grid size got: K (nt - 2 = full history) and groups per pass
+    plans = {}
+    for cfg, ctx in zip(cfgs, ctxs):
+        K, P = ctx.info.ckpt_interval, ctx.info.groups_per_pass
+        plans.setdefault(str(cfg.nx), set()).add(("full" if K >= cfg.nt - 2 else f"K {K}") + f", P {P}"
+                                                 + f" of {tomo.n_groups(cfg)}")
+    plans = {k: sorted(v) for k, v in plans.items()}
     ptrs = [t.data_ptr() for t in d_fs]
     tptrs = [t.data_ptr() for t in d_fts]
     tomo.iterate_batch(ctxs, tomo.SIRT_NORM, sched, 0, args.warmup, ptrs, tptrs)
@@ -135,10 +182,12 @@ def run_batch(args, local, rank, world, dist):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded ellipse phantoms + smoothed noise, 1% Gaussian record noise)",
             "config": {"workload": "c3: 64 phantoms of N in {128,192,256,384,512} cycling, N/2 transducers "
-                                   "r=0.43N, groups of 8, nt 10N, checkpoint ~sqrt(2 nt), plain weighted SIRT, "
+                                   "r=0.43N, groups of 8, nt 10N, memory plan timed per phantom (checkpoint interval "
+                                   "and groups per pass, see plans), plain weighted SIRT, "
                                    "all phantoms advanced together (tomo_iterate_batch)",
                        "phantoms": len(cfgs), "l2": "inputs larger than L2",
                        "parallelism": f"replicas{world}" if world > 1 else "single GPU"},
+            "plans": plans,
             "phantom_iter_per_s": world * len(cfgs) * args.steps / t_max,
             "epsilon_last_mean": float(np.nanmean(eps[:, -1])),
             "e2e": {"value": world * bytes_it * args.steps / e2e_s / 1e9, "unit": "GB/s",

@@ -74,10 +74,14 @@ typedef struct tomo_config {
     int32_t sponge_width;         /* cells */
     float sponge_max;             /* sigma at the outer edge; sigma(d)=max*((W-d)/W)^2 */
     /* execution plan */
-    int32_t ckpt_interval;        /* forward slices between checkpoints; 0 = plan picks */
+    int32_t ckpt_interval;        /* forward slices between checkpoints; 0 = plan picks
+                                     (full history when it fits, else ~sqrt(2 nt));
+                                     -1 = the fastest of full history and three intervals,
+                                     timed at tomo_create */
     int32_t groups_per_pass;      /* P of G groups resident per sweep; 0 = plan picks */
     int32_t device;               /* CUDA device ordinal */
-    int32_t reserved[4];
+    int32_t mem_limit_mb;         /* device memory the plan may use, MiB; 0 = 90 % of free */
+    int32_t reserved[3];
 } tomo_config;
 
 /* Update rules.  Each is the field update of one reference driver; all of them

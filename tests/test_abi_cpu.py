@@ -163,6 +163,45 @@ def test_header_is_c_and_links_from_c(built_lib, tmp_path):
     assert rest.startswith("invalid argument|") and len(rest) > len("invalid argument|")
 
 
+LAYOUT_CLIENT = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "tomo.h"
+#define F(s, m) printf(#s " " #m " %zu %zu\n", offsetof(s, m), sizeof(((s*)0)->m));
+int main(void) {
+    printf("tomo_config size %zu\n", sizeof(tomo_config));
+    printf("tomo_schedule size %zu\n", sizeof(tomo_schedule));
+    printf("tomo_iter_stats size %zu\n", sizeof(tomo_iter_stats));
+    printf("tomo_info size %zu\n", sizeof(tomo_info));
+    printf("tomo_noise size %zu\n", sizeof(tomo_noise));
+    %FIELDS%
+    return 0;
+}
+"""
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the header's structs have the C compiler's field offsets and sizes."""
+    structs = {"tomo_config": tomo.Config, "tomo_schedule": tomo.Schedule, "tomo_iter_stats": tomo.IterStats,
+               "tomo_info": tomo.Info, "tomo_noise": tomo.Noise}
+    fields = "\n    ".join(f"F({cn}, {name})" for cn, py in structs.items() for name, _ in py._fields_)
+    src = tmp_path / "layout.c"
+    src.write_text(LAYOUT_CLIENT.replace("%FIELDS%", fields))
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I" + os.path.join(REPO, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60).stdout.split("\n")
+    for line in filter(None, out):
+        parts = line.split()
+        py = structs[parts[0]]
+        if parts[1] == "size":
+            assert C.sizeof(py) == int(parts[2]), line
+        else:
+            d = getattr(py, parts[1])
+            assert (d.offset, d.size) == (int(parts[2]), int(parts[3])), line
+
+
 def test_bad_config_rejected_before_device(built_lib):
     for bad in (tomo.ref_config(ring_lo=1), tomo.ref_config(ring_hi=190), tomo.ref_config(group_size=0),
                 tomo.cfg_config(radius=70.0), tomo.cfg_config(courant=0.9)):

@@ -87,7 +87,9 @@ struct tomo_ctx {
     double learned_scale = 1.0;  // the network's proposal is f + learned_scale * mask * net(features)
     static constexpr int ZR = 4; // adjoint ring slots
     bool tuned = false;
+    double plan_budget = 0;      // bytes the plan's per-group buffers may take (make_plan)
     std::vector<void*> allocs;
+    std::vector<size_t> alloc_bytes;
 
     tomo_status fail(tomo_status s, const char* fmt, ...) {
         char buf[512];
@@ -109,16 +111,31 @@ struct tomo_ctx {
     template <typename T>
     tomo_status alloc(T** p, int64_t n, const char* what) {
         const size_t b = (size_t)std::max<int64_t>(n, 1) * sizeof(T);
-        allocs.push_back(nullptr);   // the slot first: a push_back that throws leaks no device memory
+        alloc_bytes.push_back(0);
+        allocs.push_back(nullptr);   // the slots first: a push_back that throws leaks no device memory
         const cudaError_t e = cudaMalloc(&allocs.back(), b);
         if (e != cudaSuccess) {
             allocs.pop_back();
+            alloc_bytes.pop_back();
             cudaGetLastError();
             return fail(TOMO_ERR_OOM, "cudaMalloc(%s, %zu bytes): %s", what, b, cudaGetErrorString(e));
         }
         bytes += (int64_t)b;
+        alloc_bytes.back() = b;
         *p = (T*)allocs.back();
         return TOMO_OK;
+    }
+    template <typename T>
+    void release(T** p) {
+        for (size_t i = 0; *p && i < allocs.size(); ++i)
+            if (allocs[i] == (void*)*p) {
+                cudaFree(allocs[i]);
+                bytes -= (int64_t)alloc_bytes[i];
+                allocs.erase(allocs.begin() + (std::ptrdiff_t)i);
+                alloc_bytes.erase(alloc_bytes.begin() + (std::ptrdiff_t)i);
+                break;
+            }
+        *p = nullptr;
     }
     // residual noise (tomo_set_residual_noise): kind 0 off, 2 a fresh draw per gradient sweep,
     // 3 one fixed draw; the key lives on the device so captured graphs see its updates
@@ -500,7 +517,48 @@ tomo_status autotune(tomo_ctx* c) {
     return TOMO_OK;
 }
 
-// Chosen memory plan.
+// Memory plan: full forward history, or checkpoints every K slices with the chunk being swept
+// recomputed; P groups resident per pass.
+struct Plan {
+    bool full;
+    int K;    // slices per chunk (nt - 2 for full history)
+    int P;    // groups per pass, 0: does not fit
+};
+
+// Device bytes one group of a pass holds under a plan: forward slots, adjoint ring, checkpoints
+// and residual records.
+double plan_bytes_per_group(const tomo_ctx* c, bool full, int K) {
+    const Geometry& g = c->geo;
+    const int64_t N = g.N, nt = g.nt;
+    const int64_t slots = full ? nt : (int64_t)K + 1;
+    const int64_t chunks = full ? 0 : (nt - 2 + K - 1) / K;
+    return 4.0 * ((double)(slots + tomo_ctx::ZR + 2 * chunks) * N + (double)nt * g.nch);
+}
+
+// The plan with the most groups per pass that fits c->plan_budget (or the configured P).
+Plan plan_of(const tomo_ctx* c, bool full, int K) {
+    const Geometry& g = c->geo;
+    Plan p{full, full ? g.nt - 2 : K, 0};
+    const double per = plan_bytes_per_group(c, full, K);
+    int P = g.cfg.groups_per_pass > 0 ? std::min(g.cfg.groups_per_pass, g.G) : g.G;
+    if (g.cfg.groups_per_pass <= 0)
+        while (P > 1 && per * P > c->plan_budget) --P;
+    p.P = per * P <= c->plan_budget ? P : 0;
+    return p;
+}
+
+void set_plan(tomo_ctx* c, const Plan& p) {
+    const int nt = c->geo.nt;
+    c->P = p.P;
+    c->full = p.full;
+    c->K = p.full ? nt - 2 : p.K;
+    c->S = p.full ? nt : p.K + 1;
+    c->nchunk = p.full ? 1 : (nt - 2 + p.K - 1) / p.K;
+}
+
+// Chosen memory plan.  ckpt_interval > 0 fixes K; 0 and -1 start from full history when it fits
+// with all groups resident, else K = ceil(sqrt(2 (nt - 2))), the interval of least memory (-1
+// then times the alternatives, tune_plan).
 tomo_status make_plan(tomo_ctx* c) {
     const Geometry& g = c->geo;
     const int64_t N = g.N, nt = g.nt, G = g.G;
@@ -509,57 +567,52 @@ tomo_status make_plan(tomo_ctx* c) {
     // fixed buffers (fields, coefficients, accumulators, records)
     const int64_t fixed = 4 * (7 * N) + 4 * (2 * G * N) + 4 * (2 * G * nt * g.nch) + 8 * (G * nt) +
                           8 * (int64_t)(G + 2) * reduce_blocks() + (int64_t)(64 << 20);
-    const double budget = 0.90 * (double)free_b - (double)fixed;
-    auto per_group = [&](bool full, int K) -> double {
-        const int64_t slots = full ? nt : (int64_t)K + 1;
-        const int64_t chunks = full ? 0 : (nt - 2 + K - 1) / K;
-        return 4.0 * ((double)(slots + 3 + 2 * chunks) * N + (double)nt * g.nch);
-    };
-    int P = g.cfg.groups_per_pass > 0 ? std::min(g.cfg.groups_per_pass, g.G) : g.G;
-    int K = g.cfg.ckpt_interval;
-    bool full;
+    double cap = 0.90 * (double)free_b;
+    if (g.cfg.mem_limit_mb > 0) cap = std::min(cap, (double)g.cfg.mem_limit_mb * (1 << 20));
+    c->plan_budget = cap - (double)fixed;
+    const int K = g.cfg.ckpt_interval;
+    Plan p{};
     if (K > 0) {
-        full = K >= nt - 2;
+        if (K < nt - 2 && K < 2) return c->fail(TOMO_ERR_ARG, "ckpt_interval must be >= 2");
+        p = plan_of(c, K >= nt - 2, K);
     } else {
-        full = per_group(true, 0) * P <= budget;
-        if (!full) K = std::max(2, (int)std::ceil(std::sqrt(2.0 * (double)(nt - 2))));
+        p = plan_of(c, true, 0);
+        if (p.P < (g.cfg.groups_per_pass > 0 ? std::min<int64_t>(g.cfg.groups_per_pass, G) : G)) p = plan_of(c, false, std::max(2, (int)std::ceil(std::sqrt(2.0 * (double)(nt - 2)))));
     }
-    if (!full && K < 2) return c->fail(TOMO_ERR_ARG, "ckpt_interval must be >= 2");
-    if (g.cfg.groups_per_pass <= 0) {
-        while (P > 1 && per_group(full, K) * P > budget) --P;
-    }
-    if (per_group(full, K) * P > budget)
-        return c->fail(TOMO_ERR_OOM, "plan needs %.2f GB for %d groups per pass, %.2f GB available",
-                       per_group(full, K) * P / 1e9, P, budget / 1e9);
-    c->P = P;
-    c->full = full;
-    if (full) {
-        c->K = (int)(nt - 2);
-        c->S = (int)nt;
-        c->nchunk = 1;
-    } else {
-        c->K = K;
-        c->S = K + 1;
-        c->nchunk = (int)((nt - 2 + K - 1) / K);
-    }
+    if (p.P < 1)
+        return c->fail(TOMO_ERR_OOM, "plan needs %.2f GB for one group per pass, %.2f GB available",
+                       plan_bytes_per_group(c, p.full, p.K) / 1e9, c->plan_budget / 1e9);
+    set_plan(c, p);
+    return TOMO_OK;
+}
+
+// The buffers whose size the plan sets (forward slots, adjoint ring, checkpoints, residual
+// records), zeroed.
+tomo_status alloc_plan_buffers(tomo_ctx* c) {
+    const Geometry& g = c->geo;
+    const int64_t N = g.N, P = c->P;
+    TRY(c->alloc(&c->hist, P * c->S * N, "forward slots"));
+    TRY(c->alloc(&c->z, P * tomo_ctx::ZR * N, "adjoint slots"));
+    if (!c->full) TRY(c->alloc(&c->ckpt, P * c->nchunk * 2 * N, "checkpoints"));
+    TRY(c->alloc(&c->rr, P * g.nt * g.nch, "residual records"));
+    CU(c, cudaMemsetAsync(c->hist, 0, sizeof(float) * (size_t)P * c->S * N, c->st));
+    CU(c, cudaMemsetAsync(c->z, 0, sizeof(float) * (size_t)P * tomo_ctx::ZR * N, c->st));
+    CU(c, cudaMemsetAsync(c->rr, 0, sizeof(float) * (size_t)(P * g.nt * g.nch), c->st));
     return TOMO_OK;
 }
 
 tomo_status create_buffers(tomo_ctx* c) {
     const Geometry& g = c->geo;
-    const int64_t N = g.N, nt = g.nt, G = g.G, P = c->P, nch = g.nch;
+    const int64_t N = g.N, nt = g.nt, G = g.G, nch = g.nch;
     TRY(c->alloc(&c->f, N, "f"));
     TRY(c->alloc(&c->ftrue, N, "f_true"));
     TRY(c->alloc(&c->coef, N, "coef"));
     TRY(c->alloc(&c->rcoef, N, "rcoef"));
     TRY(c->alloc(&c->dir, N, "dir"));
     TRY(c->alloc(&c->tmp, N, "tmp"));
-    TRY(c->alloc(&c->hist, P * c->S * N, "forward slots"));
-    TRY(c->alloc(&c->z, P * tomo_ctx::ZR * N, "adjoint slots"));
-    if (!c->full) TRY(c->alloc(&c->ckpt, P * c->nchunk * 2 * N, "checkpoints"));
+    TRY(alloc_plan_buffers(c));
     TRY(c->alloc(&c->corr, G * N, "correlation"));
     TRY(c->alloc(&c->meas, G * nt * nch, "measured records"));
-    TRY(c->alloc(&c->rr, P * nt * nch, "residual records"));
     TRY(c->alloc(&c->rpart, G * nt, "residual partials"));
     TRY(c->alloc(&c->part, (G + 2) * (int64_t)reduce_blocks(), "reduction partials"));
     TRY(c->alloc(&c->sums, G + 8, "sums"));
@@ -575,7 +628,6 @@ tomo_status create_buffers(tomo_ctx* c) {
         TRY(c->alloc(&c->rbits, (int64_t)g.ny * c->rwords, "receiver row bitmap"));
         TRY(c->alloc(&c->dmap, N, "sponge map"));
     }
-    CU(c, cudaMemsetAsync(c->rr, 0, sizeof(float) * P * nt * nch, c->st));
     CU(c, cudaMemsetAsync(c->meas, 0, sizeof(float) * G * nt * nch, c->st));
     CU(c, cudaMemsetAsync(c->rpart, 0, sizeof(double) * G * nt, c->st));
     CU(c, cudaMemsetAsync(c->f, 0, sizeof(float) * N, c->st));
@@ -616,8 +668,6 @@ tomo_status create_buffers(tomo_ctx* c) {
         d.dmap = c->dmap;
     }
     c->strip = strip_supported(d, g.cfg.profile) && !std::getenv("TOMO_NO_STRIP");
-    CU(c, cudaMemsetAsync(c->hist, 0, sizeof(float) * (size_t)P * c->S * N, c->st));
-    CU(c, cudaMemsetAsync(c->z, 0, sizeof(float) * (size_t)P * tomo_ctx::ZR * N, c->st));
     CU(c, cudaMemsetAsync(c->corr, 0, sizeof(float) * (size_t)G * N, c->st));
     CU(c, cudaStreamSynchronize(c->st));
     return TOMO_OK;
@@ -872,6 +922,115 @@ tomo_status gradient_all(tomo_ctx* c) {
     launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
     ++c->launches;
     for (int g0 = 0; g0 < g.G; g0 += c->P) TRY(run_pass(c, MODE_GRAD, g0, std::min(c->P, g.G - g0)));
+    return TOMO_OK;
+}
+
+// Replaces the plan-sized buffers by those of plan p (contents zeroed); captured graphs and the
+// kernel choice, both made for the old plan, are dropped.
+tomo_status apply_plan(tomo_ctx* c, const Plan& p) {
+    if (c->full == p.full && c->P == p.P && (p.full || c->K == p.K)) return TOMO_OK;
+    CU(c, cudaStreamSynchronize(c->st));
+    c->drop_graphs();
+    c->release(&c->hist);
+    c->release(&c->z);
+    c->release(&c->ckpt);
+    c->release(&c->rr);
+    set_plan(c, p);
+    c->tuned = false;
+    return alloc_plan_buffers(c);
+}
+
+// Cache line of a timed plan choice: the problem, then full history (0/1), K and P.
+std::string plan_key(const tomo_ctx* c) {
+    char b[160];
+    std::snprintf(b, sizeof b, "tomo-plan-1 %d %d %d %d %d %d %d", c->geo.cfg.profile, c->geo.nx, c->geo.ny,
+                  c->geo.nt, c->geo.G, c->geo.gs, c->geo.cfg.groups_per_pass);
+    return b;
+}
+
+// ckpt_interval = -1: times one gradient pass (the first P groups: forward sweep, checkpoints,
+// recompute, adjoint and correlation, as a captured graph, after one untimed pass that also
+// picks the pass's kernels) under each candidate plan that fits the budget -- full history,
+// two chunks (K = (nt - 2) / 2, half the recompute of the smallest interval), the interval of
+// least memory K = ceil(sqrt(2 (nt - 2))), and an interval whose chunk of the pass fits in half
+// the L2 (the adjoint then reads recomputed slices from L2) -- and keeps the plan of the least
+// estimated iteration time, passes x pass time.  The plans give the same results bit for bit
+// (checkpoints hold exact slices).  TOMO_TUNE_CACHE records and reuses the choice.
+tomo_status tune_plan(tomo_ctx* c) {
+    const Geometry& g = c->geo;
+    const int nt = g.nt, G = g.G;
+    std::vector<Plan> cands;
+    auto add = [&](bool full, int K) {
+        if (!full && (K < 4 || K >= nt - 2)) return;
+        const Plan p = plan_of(c, full, K);
+        if (p.P < 1) return;
+        for (const Plan& q : cands)
+            if (q.full == p.full && q.K == p.K) return;
+        cands.push_back(p);
+    };
+    const int Ks = std::max(4, (int)std::ceil(std::sqrt(2.0 * (double)(nt - 2))));
+    add(true, 0);
+    add(false, (nt - 1) / 2);
+    add(false, Ks);
+    int l2 = 0;
+    CU(c, cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->dev));
+    const Plan ps = plan_of(c, false, Ks);
+    if (ps.P >= 1) add(false, (int)(0.5 * (double)l2 / (4.0 * (double)g.N * ps.P)) - 1);
+    if (cands.empty()) return TOMO_OK;   // make_plan's plan stands
+    const char* cache = std::getenv("TOMO_TUNE_CACHE");
+    const std::string key = plan_key(c);
+    int chosen = -1;
+    if (cache && *cache) {
+        if (FILE* fp = std::fopen(cache, "r")) {
+            char line[512];
+            while (chosen < 0 && std::fgets(line, sizeof line, fp)) {
+                int full = 0, K = 0, P = 0;
+                if (std::strncmp(line, key.c_str(), key.size()) != 0 || line[key.size()] != ' ' ||
+                    std::sscanf(line + key.size(), "%d %d %d", &full, &K, &P) != 3)
+                    continue;
+                for (size_t i = 0; i < cands.size(); ++i)
+                    if (cands[i].full == (full != 0) && cands[i].K == K && cands[i].P == P) chosen = (int)i;
+            }
+            std::fclose(fp);
+        }
+    }
+    const bool tlog = std::getenv("TOMO_TUNE_LOG") != nullptr;
+    if (chosen < 0 && cands.size() == 1) chosen = 0;
+    if (chosen < 0) {
+        double best = 1e300;
+        for (size_t i = 0; i < cands.size(); ++i) {
+            const Plan& p = cands[i];
+            TRY(apply_plan(c, p));
+            launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
+            TRY(run_pass(c, MODE_GRAD, 0, p.P));
+            CU(c, cudaEventRecord(c->ev0, c->st));
+            TRY(run_pass(c, MODE_GRAD, 0, p.P));
+            CU(c, cudaEventRecord(c->ev1, c->st));
+            CU(c, cudaEventSynchronize(c->ev1));
+            float ms = 0.f;
+            CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            const double est = (double)ms * ((G + p.P - 1) / p.P);
+            if (tlog)
+                std::fprintf(stderr, "tomo tune: plan %s K %d, %d groups per pass: pass %.3f ms, iteration %.3f ms\n",
+                             p.full ? "full history" : "checkpoints", c->K, p.P, ms, est);
+            if (est < best) { best = est; chosen = (int)i; }
+        }
+        if (cache && *cache)
+            if (FILE* fp = std::fopen(cache, "a")) {
+                std::fprintf(fp, "%s %d %d %d\n", key.c_str(), cands[chosen].full ? 1 : 0, cands[chosen].K,
+                             cands[chosen].P);
+                std::fclose(fp);
+            }
+    }
+    TRY(apply_plan(c, cands[chosen]));
+    // leave the state of a fresh context
+    CU(c, cudaMemsetAsync(c->hist, 0, sizeof(float) * (size_t)c->P * c->S * g.N, c->st));
+    CU(c, cudaMemsetAsync(c->z, 0, sizeof(float) * (size_t)c->P * tomo_ctx::ZR * g.N, c->st));
+    CU(c, cudaMemsetAsync(c->rr, 0, sizeof(float) * (size_t)c->P * nt * g.nch, c->st));
+    CU(c, cudaMemsetAsync(c->corr, 0, sizeof(float) * (size_t)G * g.N, c->st));
+    CU(c, cudaMemsetAsync(c->rpart, 0, sizeof(double) * (size_t)G * nt, c->st));
+    CU(c, cudaStreamSynchronize(c->st));
+    c->launches = 0;
     return TOMO_OK;
 }
 
@@ -1157,8 +1316,9 @@ tomo_status tomo_create(const tomo_config* cfg, tomo_ctx** out) try {
     if ((s = c->cuda(cudaSetDevice(c->dev), "cudaSetDevice")) == TOMO_OK &&
         (s = c->cuda(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking), "cudaStreamCreate")) == TOMO_OK &&
         (s = c->cuda(cudaEventCreate(&c->ev0), "cudaEventCreate")) == TOMO_OK &&
-        (s = c->cuda(cudaEventCreate(&c->ev1), "cudaEventCreate")) == TOMO_OK && (s = make_plan(c.get())) == TOMO_OK)
-        s = create_buffers(c.get());
+        (s = c->cuda(cudaEventCreate(&c->ev1), "cudaEventCreate")) == TOMO_OK && (s = make_plan(c.get())) == TOMO_OK &&
+        (s = create_buffers(c.get())) == TOMO_OK && cfg->ckpt_interval < 0)
+        s = tune_plan(c.get());
     if (s != TOMO_OK) {
         g_create_error = c->err;
         return s;

@@ -50,7 +50,7 @@ class Config(C.Structure):
         ("cells_per_wavelength", C.c_float), ("sponge_width", C.c_int32),
         ("sponge_max", C.c_float),
         ("ckpt_interval", C.c_int32), ("groups_per_pass", C.c_int32), ("device", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("mem_limit_mb", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 
