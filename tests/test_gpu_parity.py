@@ -409,13 +409,16 @@ def test_two_step_kernels_match_one_step(nt, monkeypatch):
     assert rel(outs[1][0], rec_o) <= TOL_FIELD
 
 
-@pytest.mark.parametrize("shape", [(96, 70, 161, 12), (128, 128, 200, 10_000), (64, 64, 97, 9)],
-                         ids=["96x70-ckpt12", "128x128-full", "64x64-ckpt9"])
+@pytest.mark.parametrize("shape", [(96, 70, 161, 12), (128, 128, 200, 10_000), (64, 64, 97, 9), (200, 148, 120, 4)],
+                         ids=["96x70-ckpt12", "128x128-full", "64x64-ckpt9", "200x148-ckpt4"])
 @pytest.mark.parametrize("tile", ["1", "f", "a"])
-def test_tile_kernels_match_strip_kernels(shape, tile, monkeypatch):
+@pytest.mark.parametrize("warps", ["16", "10"], ids=["48x48", "48x24"])
+def test_tile_kernels_match_strip_kernels(shape, tile, warps, monkeypatch):
     """The multi-step tile kernels (forward launches of up to 8 steps, adjoint launches of 6, 2 and
-    1 steps, with redundant halo cells) give the strip kernels' records, gradients and residual bit
-    for bit: ragged tiles (70 rows), checkpointed and resident histories, passes of fewer groups."""
+    1 steps, with redundant halo cells; 48 x 48 and 48 x 24 owned tiles) give the strip kernels'
+    records, gradients and residual bit for bit: ragged tiles (70 rows; 200 x 148 cells), checkpointed
+    and resident histories (K = 4: five slots, forward launches of at most three steps), passes of
+    fewer groups."""
     nx, ny, nt, K = shape
     kw = dict(nx=nx, ny=ny, nt=nt, n_transducers=28, radius=min(nx, ny) / 2 - 6, ckpt_interval=K)
     fo = blob_phantom(ny, nx, seed=58)
@@ -427,13 +430,18 @@ def test_tile_kernels_match_strip_kernels(shape, tile, monkeypatch):
         monkeypatch.setenv("TOMO_FWD_PAIR", "0")
         monkeypatch.setenv("TOMO_ADJ_PAIR", "0")
         monkeypatch.setenv("TOMO_TILE", t)
+        monkeypatch.setenv("TOMO_TILE_WARPS", warps)
         for P in (0, 3):
             with tomo.Context(small_cfg(groups_per_pass=P, **kw)) as ctx:
                 rec = ctx.forward(fo)
                 dfg, _, r2 = ctx.gradient(f0, meas)
-            outs.append((rec, dfg, r2))
+                # kernels per iteration: the tile run must really have taken the tile kernels
+                f = np.zeros_like(fo)
+                launches = ctx.iterate(tomo.SIRT_CLASSIC, tomo.schedule(omega=0.0), 0, f, None).kernel_launches
+            outs.append((rec, dfg, r2, launches))
     for o in outs[1:]:
         assert np.array_equal(outs[0][0], o[0])
         assert np.array_equal(outs[0][1], o[1])
         assert outs[0][2] == o[2]
+    assert outs[2][3] < outs[0][3] and outs[3][3] < outs[1][3], [o[3] for o in outs]
     assert rel(outs[-1][0], meas) <= TOL_FIELD

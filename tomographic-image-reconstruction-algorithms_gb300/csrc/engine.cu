@@ -79,13 +79,19 @@ struct tomo_ctx {
     bool tile_adj = false;       // ... and for the adjoint sweeps
     bool tile_fwd1 = false;      // the same choices for passes of one group (ART)
     bool tile_adj1 = false;
-    static constexpr int TILE_FWD_STEPS = 8;   // steps per forward tile launch
+    int tile_warps_fwd = 16, tile_warps_adj = 16;     // tile shape: 16 warps (48 x 48) or 10 (48 x 24)
+    int tile_warps_fwd1 = 16, tile_warps_adj1 = 16;   // ... for passes of one group
     // learned iteration (allocated on first use)
     float *illum = nullptr, *feat = nullptr, *fsave = nullptr, *dnet = nullptr, *dsave = nullptr;
     unsigned int *illum_max = nullptr, *maxsave = nullptr;
     bool illum_ready = false;
     double learned_scale = 1.0;  // the network's proposal is f + learned_scale * mask * net(features)
     static constexpr int ZR = 4; // adjoint ring slots
+    TileMaps tmaps;              // TMA maps of hist, z, coef, dmap, rid (tile kernels)
+    unsigned int* err_host = nullptr;   // tile kernels' wait time-out word (mapped pinned memory)
+    unsigned int* err_dev = nullptr;
+    uint64_t wait_ns = 1000000000ull;   // bound of every tile-kernel copy wait (TOMO_WAIT_LIMIT_NS)
+    uint32_t test_tx = 0;        // TOMO_TEST_UNDELIVERED_TX: bytes a region barrier expects in vain
     bool tuned = false;
     double plan_budget = 0;      // bytes the plan's per-group buffers may take (make_plan)
     std::vector<void*> allocs;
@@ -151,6 +157,7 @@ struct tomo_ctx {
         if (dev >= 0) cudaSetDevice(dev);
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
         for (void* p : allocs) cudaFree(p);
+        if (err_host) cudaFreeHost(err_host);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (st) cudaStreamDestroy(st);
@@ -228,6 +235,8 @@ TileFwd tile_fwd_args(tomo_ctx* c, int k0, int T, int g0, int ng) {
     a.ng = ng;
     a.K = std::max(c->K, 1);
     a.nchunk = c->nchunk;
+    a.warps = ng == 1 ? c->tile_warps_fwd1 : c->tile_warps_fwd;
+    a.w = TileWait{c->err_dev, c->wait_ns, c->test_tx};
     return a;
 }
 
@@ -247,7 +256,38 @@ TileAdj tile_adj_args(tomo_ctx* c, int kz0, int T, int g0, int ng) {
     a.kz0 = kz0;
     a.T = T;
     a.ng = ng;
+    a.warps = ng == 1 ? c->tile_warps_adj1 : c->tile_warps_adj;
+    a.w = TileWait{c->err_dev, c->wait_ns, c->test_tx};
     return a;
+}
+
+// Forward steps of the next tile launch when L remain: at most 8, and at most S - 2 so the
+// slices it writes never land on the two slots it reads.
+int tile_fwd_steps(const tomo_ctx* c, int L) { return std::min(std::min(L, TILE_MAX_FWD), c->S - 2); }
+
+bool tiles_ok(const tomo_ctx* c) { return tile_supported(c->dg, c->geo.cfg.profile) && c->tmaps.ok; }
+
+// (Re)encodes the tile kernels' TMA maps for the current buffers; tiles stay off without them.
+void encode_maps(tomo_ctx* c) {
+    std::string why;
+    if (!tile_supported(c->dg, c->geo.cfg.profile) ||
+        !encode_tile_maps(&c->tmaps, c->dg, c->hist, (int64_t)c->P * c->S, c->z, (int64_t)c->P * tomo_ctx::ZR,
+                          c->coef, &why)) {
+        c->tmaps.ok = false;
+        c->tile_fwd = c->tile_adj = c->tile_fwd1 = c->tile_adj1 = false;
+        if (!why.empty() && std::getenv("TOMO_TUNE_LOG")) std::fprintf(stderr, "tomo: tile kernels off: %s\n", why.c_str());
+    }
+}
+
+// Stream synchronisation that also reports a tile kernel's timed-out copy wait.
+tomo_status sync_check(tomo_ctx* c) {
+    CU(c, cudaStreamSynchronize(c->st));
+    if (c->err_host && *(volatile unsigned int*)c->err_host) {
+        *(volatile unsigned int*)c->err_host = 0u;
+        return c->fail(TOMO_ERR_TIMEOUT, "tile kernel: a TMA copy did not arrive within %llu ns",
+                       (unsigned long long)c->wait_ns);
+    }
+    return TOMO_OK;
 }
 
 // Steps of the next tile adjoint launch when L steps remain: 6, 2 or 1 (the step counts whose
@@ -270,16 +310,21 @@ bool tune_cache_read(tomo_ctx* c, const char* path) {
     bool hit = false;
     while (!hit && std::fgets(line, sizeof line, fp)) {
         if (std::strncmp(line, key.c_str(), key.size()) != 0 || line[key.size()] != ' ') continue;
-        int v[11] = {0};
-        const int nv = std::sscanf(line + key.size(), "%d %d %d %d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2],
-                                   &v[3], &v[4], &v[5], &v[6], &v[7], &v[8], &v[9], &v[10]);
-        if (nv == 7 || nv == 9 || nv == 11) {
+        int v[15] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 16, 16, 16, 16};
+        const int nv = std::sscanf(line + key.size(), "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &v[0], &v[1],
+                                   &v[2], &v[3], &v[4], &v[5], &v[6], &v[7], &v[8], &v[9], &v[10], &v[11], &v[12],
+                                   &v[13], &v[14]);
+        if (nv == 7 || nv == 9 || nv == 11 || nv == 15) {
             c->rows_fwd = v[0]; c->rows_adj = v[1]; c->adj_variant = v[2]; c->adj_pair = v[3] != 0;
             c->rows_adj2 = v[4]; c->fwd_pair = v[5] != 0 && c->S >= 4; c->rows_fwd2 = v[6];
-            c->tile_fwd = v[7] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
-            c->tile_adj = v[8] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
-            c->tile_fwd1 = v[9] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
-            c->tile_adj1 = v[10] != 0 && tile_supported(c->dg, c->geo.cfg.profile);
+            c->tile_fwd = v[7] != 0 && tiles_ok(c);
+            c->tile_adj = v[8] != 0 && tiles_ok(c);
+            c->tile_fwd1 = v[9] != 0 && tiles_ok(c);
+            c->tile_adj1 = v[10] != 0 && tiles_ok(c);
+            c->tile_warps_fwd = v[11] == 10 ? 10 : 16;
+            c->tile_warps_adj = v[12] == 10 ? 10 : 16;
+            c->tile_warps_fwd1 = v[13] == 10 ? 10 : 16;
+            c->tile_warps_adj1 = v[14] == 10 ? 10 : 16;
             hit = true;
         }
     }
@@ -290,20 +335,26 @@ bool tune_cache_read(tomo_ctx* c, const char* path) {
 void tune_cache_append(const tomo_ctx* c, const char* path) {
     FILE* fp = std::fopen(path, "a");
     if (!fp) return;
-    std::fprintf(fp, "%s %d %d %d %d %d %d %d %d %d %d %d\n", tune_key(c).c_str(), c->rows_fwd, c->rows_adj,
-                 c->adj_variant, c->adj_pair ? 1 : 0, c->rows_adj2, c->fwd_pair ? 1 : 0, c->rows_fwd2,
-                 c->tile_fwd ? 1 : 0, c->tile_adj ? 1 : 0, c->tile_fwd1 ? 1 : 0, c->tile_adj1 ? 1 : 0);
+    std::fprintf(fp, "%s %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d\n", tune_key(c).c_str(), c->rows_fwd,
+                 c->rows_adj, c->adj_variant, c->adj_pair ? 1 : 0, c->rows_adj2, c->fwd_pair ? 1 : 0, c->rows_fwd2,
+                 c->tile_fwd ? 1 : 0, c->tile_adj ? 1 : 0, c->tile_fwd1 ? 1 : 0, c->tile_adj1 ? 1 : 0,
+                 c->tile_warps_fwd, c->tile_warps_adj, c->tile_warps_fwd1, c->tile_warps_adj1);
     std::fclose(fp);
 }
 
 // TOMO_TILE=0 / 1 / f / a turns the multi-step tile kernels off, on for both sweeps, on for the
-// forward or the adjoint sweeps only (tests and profiling).
+// forward or the adjoint sweeps only; TOMO_TILE_WARPS=16 / 10 fixes the tile shape (tests and
+// profiling).
 void tile_override(tomo_ctx* c) {
     const char* e = std::getenv("TOMO_TILE");
     if (!e || !*e) return;
-    const bool ok = tile_supported(c->dg, c->geo.cfg.profile);
+    const bool ok = tiles_ok(c);
     c->tile_fwd = c->tile_fwd1 = ok && (e[0] == '1' || e[0] == 'f');
     c->tile_adj = c->tile_adj1 = ok && (e[0] == '1' || e[0] == 'a');
+    if (const char* w = std::getenv("TOMO_TILE_WARPS")) {
+        const int warps = std::atoi(w) == 10 ? 10 : 16;
+        c->tile_warps_fwd = c->tile_warps_adj = c->tile_warps_fwd1 = c->tile_warps_adj1 = warps;
+    }
 }
 
 // Picks the strip kernels (rows per warp, register variant, one or two steps
@@ -426,33 +477,58 @@ tomo_status autotune(tomo_ctx* c) {
     c->rows_fwd = rows_f1;
     c->rows_fwd2 = code_f2;
     c->fwd_pair = best_f2 < 0.97f * best_f1;
-    // multi-step tile kernels against the chosen strip kernels, per step: a forward launch of 8
-    // steps and adjoint launches of 6 + 2 steps
-    if (tile_supported(c->dg, c->geo.cfg.profile)) {
+    // multi-step tile kernels against the chosen strip kernels, per step: forward launches of 8
+    // steps and adjoint launches of 6 + 2 steps, for each tile shape (48 x 48 or 48 x 24 owned)
+    if (tiles_ok(c)) {
+        auto time_tiles = [&](int n, int warps, float& tf, float& ta) -> tomo_status {
+            tf = ta = 1e30f;
+            for (int pass = 0; pass < passes; ++pass) {
+                float t_ms = 0.f;
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                for (int t = 0; t < reps; t += tile_fwd_steps(c, reps - t)) {
+                    TileFwd fa = tile_fwd_args(c, k0 + t, tile_fwd_steps(c, reps - t), 0, n);
+                    fa.warps = warps;
+                    launch_fwd_tile(c->dg, c->tmaps, fa, c->st);
+                }
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) tf = std::min(tf, t_ms);
+                CU(c, cudaEventRecord(c->ev0, c->st));
+                for (const int kz : {k0 + reps + 1, k0 + reps - 5}) {
+                    TileAdj aa = tile_adj_args(c, kz, kz == k0 + reps + 1 ? 6 : 2, 0, n);
+                    aa.warps = warps;
+                    launch_adj_tile(c->dg, c->tmaps, aa, c->st);
+                }
+                CU(c, cudaEventRecord(c->ev1, c->st));
+                CU(c, cudaEventSynchronize(c->ev1));
+                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
+                if (pass > 0) ta = std::min(ta, t_ms);
+            }
+            if (tlog)
+                std::fprintf(stderr, "tomo tune: %d-group tiles of %d warps: forward %.2f us/step, adjoint %.2f us/step\n",
+                             n, warps, 1e3 * tf / reps, 1e3 * ta / reps);
+            return TOMO_OK;
+        };
+        // the faster shape per sweep for passes of n groups
+        auto best_tiles = [&](int n, float& tf, float& ta, int& wf, int& wa) -> tomo_status {
+            tf = ta = 1e30f;
+            for (const int warps : {16, 10}) {
+                float f = 0.f, a = 0.f;
+                TRY(time_tiles(n, warps, f, a));
+                if (f < tf) { tf = f; wf = warps; }
+                if (a < ta) { ta = a; wa = warps; }
+            }
+            return TOMO_OK;
+        };
         float ms_tf = 1e30f, ms_ta = 1e30f;
-        for (int pass = 0; pass < passes; ++pass) {
-            CU(c, cudaEventRecord(c->ev0, c->st));
-            launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, k0, reps, 0, ng), c->st);
-            CU(c, cudaEventRecord(c->ev1, c->st));
-            CU(c, cudaEventSynchronize(c->ev1));
-            float t_ms = 0.f;
-            CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
-            if (pass > 0) ms_tf = std::min(ms_tf, t_ms);
-            CU(c, cudaEventRecord(c->ev0, c->st));
-            launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + reps + 1, 6, 0, ng), c->st);
-            launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + reps - 5, 2, 0, ng), c->st);
-            CU(c, cudaEventRecord(c->ev1, c->st));
-            CU(c, cudaEventSynchronize(c->ev1));
-            CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
-            if (pass > 0) ms_ta = std::min(ms_ta, t_ms);
-        }
-        if (tlog)
-            std::fprintf(stderr, "tomo tune: tile forward %.2f us/step, tile adjoint %.2f us/step\n",
-                         1e3 * ms_tf / reps, 1e3 * ms_ta / reps);
+        TRY(best_tiles(ng, ms_tf, ms_ta, c->tile_warps_fwd, c->tile_warps_adj));
         c->tile_fwd = ms_tf < 0.97f * std::min(best_f1, c->fwd_pair ? best_f2 : best_f1);
         c->tile_adj = ms_ta < 0.97f * best_a;
         c->tile_fwd1 = c->tile_fwd;
         c->tile_adj1 = c->tile_adj;
+        c->tile_warps_fwd1 = c->tile_warps_fwd;
+        c->tile_warps_adj1 = c->tile_warps_adj;
         if (c->geo.G > 1) {
             // passes of one group (ART): the chosen strip kernels against the tiles, 8 steps each
             float s_f = 1e30f, s_a = 1e30f, t_f = 1e30f, t_a = 1e30f;
@@ -489,20 +565,8 @@ tomo_status autotune(tomo_ctx* c) {
                 CU(c, cudaEventSynchronize(c->ev1));
                 CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
                 if (pass > 0) s_a = std::min(s_a, t_ms);
-                CU(c, cudaEventRecord(c->ev0, c->st));
-                launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, k0, reps, 0, 1), c->st);
-                CU(c, cudaEventRecord(c->ev1, c->st));
-                CU(c, cudaEventSynchronize(c->ev1));
-                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
-                if (pass > 0) t_f = std::min(t_f, t_ms);
-                CU(c, cudaEventRecord(c->ev0, c->st));
-                launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + reps + 1, 6, 0, 1), c->st);
-                launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + reps - 5, 2, 0, 1), c->st);
-                CU(c, cudaEventRecord(c->ev1, c->st));
-                CU(c, cudaEventSynchronize(c->ev1));
-                CU(c, cudaEventElapsedTime(&t_ms, c->ev0, c->ev1));
-                if (pass > 0) t_a = std::min(t_a, t_ms);
             }
+            TRY(best_tiles(1, t_f, t_a, c->tile_warps_fwd1, c->tile_warps_adj1));
             if (tlog)
                 std::fprintf(stderr, "tomo tune: one group: strip forward %.2f / tile %.2f us/step, strip adjoint "
                              "%.2f / tile %.2f us/step\n", 1e3 * s_f / reps, 1e3 * t_f / reps, 1e3 * s_a / reps,
@@ -645,9 +709,9 @@ tomo_status create_buffers(tomo_ctx* c) {
                 bits[(size_t)(q / g.nx) * c->rwords + (b >> 5)] |= 1u << (b & 31);
             }
         CU(c, cudaMemcpyAsync(c->rbits, bits.data(), sizeof(uint32_t) * bits.size(), cudaMemcpyHostToDevice, c->st));
-        CU(c, cudaStreamSynchronize(c->st));   // `bits` is local
+        TRY(sync_check(c));   // `bits` is local
     }
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     DevGeo& d = c->dg;
     d.nx = g.nx; d.ny = g.ny; d.nt = g.nt; d.nch = g.nch;
     d.lo = g.lo; d.hi = g.hi; d.gs = g.gs;
@@ -664,12 +728,19 @@ tomo_status create_buffers(tomo_ctx* c) {
                 if (dd < d.sponge_w) dm[(size_t)j * g.nx + i] = d.damp[dd];
             }
         CU(c, cudaMemcpyAsync(c->dmap, dm.data(), sizeof(float) * N, cudaMemcpyHostToDevice, c->st));
-        CU(c, cudaStreamSynchronize(c->st));   // `dm` is local
+        TRY(sync_check(c));   // `dm` is local
         d.dmap = c->dmap;
     }
     c->strip = strip_supported(d, g.cfg.profile) && !std::getenv("TOMO_NO_STRIP");
+    // the tile kernels' wait time-out word, written by the device, read by sync_check
+    CU(c, cudaHostAlloc((void**)&c->err_host, sizeof(unsigned int), cudaHostAllocMapped));
+    *c->err_host = 0u;
+    CU(c, cudaHostGetDevicePointer((void**)&c->err_dev, c->err_host, 0));
+    if (const char* e = std::getenv("TOMO_WAIT_LIMIT_NS")) c->wait_ns = std::strtoull(e, nullptr, 10);
+    if (const char* e = std::getenv("TOMO_TEST_UNDELIVERED_TX")) c->test_tx = (uint32_t)std::strtoul(e, nullptr, 10);
+    encode_maps(c);
     CU(c, cudaMemsetAsync(c->corr, 0, sizeof(float) * (size_t)G * N, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     return TOMO_OK;
 }
 
@@ -712,7 +783,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     if (tile_fwd) {
         // multi-step tile launches: every slice 2 .. nt-1 is recorded by the launch computing it
         for (int k = 1; k <= nt - 2;) {
-            const int T = std::min(tomo_ctx::TILE_FWD_STEPS, nt - 1 - k);
+            const int T = tile_fwd_steps(c, nt - 1 - k);
             TileFwd a = tile_fwd_args(c, k, T, g0, ng);
             if (mode == MODE_GRAD && !c->full) {
                 a.ckpt = c->ckpt;
@@ -720,7 +791,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
             }
             a.gmeas = resid ? meas_g : nullptr;
             a.gout = out_g;
-            launch_fwd_tile(c->dg, c->coef, a, st);
+            launch_fwd_tile(c->dg, c->tmaps, a, st);
             ++n;
             k += T;
         }
@@ -823,8 +894,8 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
                 }
                 for (int m = qa + 1; m <= qb;) {
                     if (tile_fwd) {
-                        const int T = std::min(tomo_ctx::TILE_FWD_STEPS, qb - m + 1);
-                        launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, m - 1, T, g0, ng), st);
+                        const int T = tile_fwd_steps(c, qb - m + 1);
+                        launch_fwd_tile(c->dg, c->tmaps, tile_fwd_args(c, m - 1, T, g0, ng), st);
                         m += T;
                     } else if (c->strip && c->fwd_pair && m + 1 <= qb) {
                         launch_fwd2_strip(c->rows_fwd2, c->dg, c->coef, fwd_args(c, m - 1, g0, ng),
@@ -841,7 +912,7 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
         for (int q = qb; q >= qa;) {
             if (tile_adj) {
                 const int T = tile_adj_steps(q - qa + 1);
-                launch_adj_tile(c->dg, c->coef, tile_adj_args(c, q + 1, T, g0, ng), st);
+                launch_adj_tile(c->dg, c->tmaps, tile_adj_args(c, q + 1, T, g0, ng), st);
                 q -= T;
             } else if (c->adj_pair && q - 1 >= qa) {
                 launch_adj2_strip(c->rows_adj2, c->dg, c->coef, adj_args(c, q, g0, ng), adj_args(c, q - 1, g0, ng), st);
@@ -929,7 +1000,7 @@ tomo_status gradient_all(tomo_ctx* c) {
 // kernel choice, both made for the old plan, are dropped.
 tomo_status apply_plan(tomo_ctx* c, const Plan& p) {
     if (c->full == p.full && c->P == p.P && (p.full || c->K == p.K)) return TOMO_OK;
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     c->drop_graphs();
     c->release(&c->hist);
     c->release(&c->z);
@@ -937,7 +1008,9 @@ tomo_status apply_plan(tomo_ctx* c, const Plan& p) {
     c->release(&c->rr);
     set_plan(c, p);
     c->tuned = false;
-    return alloc_plan_buffers(c);
+    TRY(alloc_plan_buffers(c));
+    encode_maps(c);
+    return TOMO_OK;
 }
 
 // Cache line of a timed plan choice: the problem, then full history (0/1), K and P.
@@ -1029,7 +1102,7 @@ tomo_status tune_plan(tomo_ctx* c) {
     CU(c, cudaMemsetAsync(c->rr, 0, sizeof(float) * (size_t)c->P * nt * g.nch, c->st));
     CU(c, cudaMemsetAsync(c->corr, 0, sizeof(float) * (size_t)G * g.N, c->st));
     CU(c, cudaMemsetAsync(c->rpart, 0, sizeof(double) * (size_t)G * nt, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     c->launches = 0;
     return TOMO_OK;
 }
@@ -1071,7 +1144,7 @@ tomo_status epsilon(tomo_ctx* c, double* out) {
     c->launches += 2;
     double ab[2];
     CU(c, cudaMemcpyAsync(ab, c->sums + 2, sizeof ab, cudaMemcpyDeviceToHost, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     *out = 100.0 * std::sqrt(ab[0]) / std::sqrt(ab[1]);
     return TOMO_OK;
 }
@@ -1105,7 +1178,7 @@ tomo_status update_core(tomo_ctx* c, int method, const tomo_schedule* sch, doubl
         c->launches += 3;
         std::vector<double> d2(G);
         CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
-        CU(c, cudaStreamSynchronize(c->st));
+        TRY(sync_check(c));
         std::vector<double> w(G);
         double W = 0.0;
         for (int gg = 0; gg < G; ++gg) { w[gg] = 1.0 / std::sqrt(d2[gg]); W += w[gg]; }
@@ -1114,7 +1187,7 @@ tomo_status update_core(tomo_ctx* c, int method, const tomo_schedule* sch, doubl
         launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
         ++c->launches;
         TRY(apply_dir(c, sch, s));
-        CU(c, cudaStreamSynchronize(c->st));   // w lives on the host stack
+        TRY(sync_check(c));   // w lives on the host stack
         break;
     }
     case TOMO_SIRT_AVG_WEIGHT: {
@@ -1173,7 +1246,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
             TRY(apply_dir(c, sch, s));
         }
         TRY(residual_norm(c, &acc));
-        CU(c, cudaStreamSynchronize(c->st));
+        TRY(sync_check(c));
         r2 = acc;
     } else {
         TRY(gradient_all(c));
@@ -1183,7 +1256,7 @@ tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int 
     CU(c, cudaEventRecord(c->ev1, c->st));
     double eps = std::numeric_limits<double>::quiet_NaN();
     if (have_true) TRY(epsilon(c, &eps));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     CU(c, cudaGetLastError());
     fill_stats(c, stats, eps, r2, s, (double)G, launches0);
     return TOMO_OK;
@@ -1201,13 +1274,13 @@ tomo_status norm_direction(tomo_ctx* c) {
     launch_sum_parts(c->part, G, nb, c->sums, c->st);
     std::vector<double> d2(G), w(G);
     CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     double W = 0.0;
     for (int gg = 0; gg < G; ++gg) { w[gg] = 1.0 / std::sqrt(d2[gg]); W += w[gg]; }
     for (int gg = 0; gg < G; ++gg) w[gg] /= W;
     CU(c, cudaMemcpyAsync(c->sums, w.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
     launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     c->launches += 4;
     return TOMO_OK;
 }
@@ -1233,7 +1306,7 @@ tomo_status compute_illumination(tomo_ctx* c) {
     launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, g.N, g.cfg.courant, c->st);
     for (int g0 = 0; g0 < g.G; g0 += c->P) TRY(run_pass(c, MODE_ILLUM, g0, std::min(c->P, g.G - g0)));
     launch_maxabs(c->illum, c->mask, g.N, c->illum_max, c->st);
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     c->illum_ready = true;
     return TOMO_OK;
 }
@@ -1375,7 +1448,7 @@ tomo_status tomo_forward(tomo_ctx* c, const float* f, float* records, float* u_l
     TRY(forward_all(c, u_last));
     CU(c, cudaMemcpyAsync(records, c->rec, sizeof(float) * (size_t)g.G * c->recs_per_group(),
                           cudaMemcpyDeviceToHost, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     CU(c, cudaGetLastError());
     return TOMO_OK;
 } catch (...) {
@@ -1403,7 +1476,7 @@ tomo_status tomo_set_residual_noise(tomo_ctx* c, const tomo_noise* noise) try {
         return c->fail(TOMO_ERR_ARG, "residual noise level must be in [0, 1)");
     CU(c, cudaSetDevice(c->dev));
     if (kind != 0 && !c->noise_key) TRY(c->alloc(&c->noise_key, 1, "noise key"));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     c->noise_kind = kind;
     c->noise_seed = noise ? noise->seed : 0;
     c->noise_draws = 0;
@@ -1413,7 +1486,7 @@ tomo_status tomo_set_residual_noise(tomo_ctx* c, const tomo_noise* noise) try {
     c->dg.noise_key = kind != 0 ? c->noise_key : nullptr;
     c->dg.noise_level = kind != 0 ? noise->level : 0.f;
     c->drop_graphs();                       // captured launches hold the old DevGeo
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     return TOMO_OK;
 } catch (...) {
     return abi_exception(c ? &c->err : nullptr);
@@ -1424,7 +1497,7 @@ tomo_status tomo_set_records(tomo_ctx* c, const float* records) try {
     CU(c, cudaSetDevice(c->dev));
     CU(c, cudaMemcpyAsync(c->meas, records, sizeof(float) * (size_t)c->geo.G * c->recs_per_group(),
                           cudaMemcpyHostToDevice, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     c->meas_set = true;
     return TOMO_OK;
 } catch (...) {
@@ -1452,7 +1525,7 @@ tomo_status tomo_gradient(tomo_ctx* c, const float* f, const float* records, flo
         launch_combine(c->corr, g.G, g.N, c->f, g.corr_scale, nullptr, 1.0, c->dir, c->st);
         CU(c, cudaMemcpyAsync(df, c->dir, sizeof(float) * g.N, cudaMemcpyDeviceToHost, c->st));
     }
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     CU(c, cudaGetLastError());
     return TOMO_OK;
 } catch (...) {
@@ -1470,7 +1543,7 @@ tomo_status tomo_iterate(tomo_ctx* c, int32_t method, const tomo_schedule* sched
     if (f_true) CU(c, cudaMemcpyAsync(c->ftrue, f_true, sizeof(float) * g.N, cudaMemcpyHostToDevice, c->st));
     TRY(iterate_core(c, method, sched, iter, f_true != nullptr, stats));
     CU(c, cudaMemcpyAsync(f_inout, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToHost, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     return TOMO_OK;
 } catch (...) {
     return abi_exception(c ? &c->err : nullptr);
@@ -1500,7 +1573,7 @@ tomo_status tomo_run(tomo_ctx* c, int32_t method, const tomo_schedule* sched, fl
         prev = st.epsilon;
     }
     CU(c, cudaMemcpyAsync(f_inout, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToHost, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     if (iters_done) *iters_done = done;
     if (result == TOMO_ERR_DIVERGED) c->err = "epsilon rose or became NaN";
     return result;
@@ -1558,7 +1631,7 @@ tomo_status tomo_gradient_groups_device(tomo_ctx* c, const float* d_f, int32_t g
         ++c->launches;
         CU(c, cudaMemcpyAsync(resid_norm2, c->sums, sizeof(double), cudaMemcpyDeviceToHost, c->st));
     }
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     CU(c, cudaGetLastError());
     return TOMO_OK;
 } catch (...) {
@@ -1607,7 +1680,7 @@ tomo_status tomo_update_device(tomo_ctx* c, int32_t method, const tomo_schedule*
     double eps = std::numeric_limits<double>::quiet_NaN();
     if (d_f_true) TRY(epsilon(c, &eps));
     CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * g.N, cudaMemcpyDeviceToDevice, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     CU(c, cudaGetLastError());
     fill_stats(c, stats, eps, std::numeric_limits<double>::quiet_NaN(), s, 0.0, launches0);
     return TOMO_OK;
@@ -1624,7 +1697,7 @@ tomo_status tomo_features_device(tomo_ctx* c, const float* d_f, float* d_feat, d
     double r2 = 0.0;
     TRY(features_core(c, &r2));
     CU(c, cudaMemcpyAsync(d_feat, c->feat, sizeof(float) * 3 * N, cudaMemcpyDeviceToDevice, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     if (resid_norm2) *resid_norm2 = r2;
     return TOMO_OK;
 } catch (...) {
@@ -1668,7 +1741,7 @@ tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule
     double eps = std::numeric_limits<double>::quiet_NaN();
     if (d_f_true) TRY(epsilon(c, &eps));
     CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     CU(c, cudaGetLastError());
     if (accepted) *accepted = ok ? 1 : 0;
     if (stats) {
@@ -1746,7 +1819,7 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
         if (d_f_true && eps <= target_epsilon) break;
     }
     CU(c, cudaMemcpyAsync(d_f, c->f, fb, cudaMemcpyDeviceToDevice, c->st));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     CU(c, cudaGetLastError());
     if (iters_done) *iters_done = done;
     if (sweeps) *sweeps = nsweep;
@@ -1775,12 +1848,12 @@ tomo_status tomo_time_kernel(tomo_ctx* c, int32_t which, int32_t steps, double* 
     CU(c, cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
     for (int t = 0; t < steps;) {
         if (which == 0 && c->tile_fwd) {
-            const int T = std::min(tomo_ctx::TILE_FWD_STEPS, steps - t);
-            launch_fwd_tile(c->dg, c->coef, tile_fwd_args(c, k0 + t, T, 0, ng), c->st);
+            const int T = tile_fwd_steps(c, steps - t);
+            launch_fwd_tile(c->dg, c->tmaps, tile_fwd_args(c, k0 + t, T, 0, ng), c->st);
             t += T;
         } else if (which == 1 && c->tile_adj) {
             const int T = tile_adj_steps(steps - t);
-            launch_adj_tile(c->dg, c->coef, tile_adj_args(c, k0 + steps - t, T, 0, ng), c->st);
+            launch_adj_tile(c->dg, c->tmaps, tile_adj_args(c, k0 + steps - t, T, 0, ng), c->st);
             t += T;
         } else if (which == 0 && c->fwd_pair && t + 1 < steps) {
             launch_fwd2_strip(c->rows_fwd2, c->dg, c->coef, fwd_args(c, k0 + t, 0, ng), fwd_args(c, k0 + t + 1, 0, ng),
@@ -1874,7 +1947,7 @@ tomo_status tomo_set_learned_scale(tomo_ctx* c, double scale) {
 tomo_status tomo_synchronize(tomo_ctx* c) try {
     if (!c) return TOMO_ERR_ARG;
     CU(c, cudaSetDevice(c->dev));
-    CU(c, cudaStreamSynchronize(c->st));
+    TRY(sync_check(c));
     CU(c, cudaGetLastError());
     return TOMO_OK;
 } catch (...) {

@@ -249,20 +249,31 @@ void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, 
 // slices k0+1 .. k0+T (T <= 8) of every group of the pass, writes each to its slot, its
 // checkpoint copy and its records; an adjoint launch computes z(kz0) .. z(kz0-T+1) (T in
 // {1, 2, 6}) with the correlation, writing the last two slices to the ring.
+// Bounded waits of the tile kernels' TMA copies: a block that waits longer than wait_ns for a
+// copy sets bit 0 of *err (host-visible) and leaves the launch.  extra_tx (0 in production)
+// makes the region copy's barrier expect bytes that never arrive, so a test can run the wait
+// out and check the status.
+struct TileWait {
+    unsigned int* err;
+    uint64_t wait_ns;
+    uint32_t extra_tx;
+};
 struct TileFwd {
     float* hist;         // forward slots of pass-group 0; slice m at slot m % S
-    int64_t gstride;
+    int64_t gstride;     // S * N: group gl's slot s is plane gl * S + s of the slot tensor
     int S;
-    int k0, T;
+    int k0, T;           // computes slices k0+1 .. k0+T; T <= 8 and T <= S - 2
     int g0, ng;
     float* ckpt;         // checkpoint copies (null: none): chunk ch >= 1 keeps slices ch K - 1 .. ch K
     int64_t ckstride;
     int K, nchunk;
     const float* gmeas;  // measured records of pass-group 0 (null: simulate)
     float* gout;         // records / residual of pass-group 0 (slices >= 2)
+    int warps;           // tile shape: 16 (48 x 48 owned cells) or 10 (48 x 24)
+    TileWait w;
 };
 struct TileAdj {
-    float* z;            // adjoint ring of pass-group 0: z(m) at slot m % 4
+    float* z;            // adjoint ring of pass-group 0: z(m) at slot m % 4 (plane gl * 4 + slot)
     int64_t zstride;
     const float* hist;   // forward slots of pass-group 0: u(m-1) at slot (m-1) % S
     int64_t ustride;
@@ -273,9 +284,24 @@ struct TileAdj {
     int64_t cstride;
     int kz0, T;
     int ng;
+    int warps;           // tile shape: 16 (48 x 48 owned cells) or 10 (48 x 24)
+    TileWait w;
+};
+// TMA tensor maps of one context's buffers (forward slots, adjoint ring, coefficient, sponge
+// map, receiver map) for each tile shape, encoded on the host by encode_tile_maps; opaque
+// outside tile.cu.
+struct TileMaps {
+    alignas(64) unsigned char raw[2][6][128];
+    bool ok = false;
 };
 bool tile_supported(const DevGeo& g, int profile);
-void launch_fwd_tile(const DevGeo& g, const float* coef, const TileFwd& a, void* stream);
-void launch_adj_tile(const DevGeo& g, const float* coef, const TileAdj& a, void* stream);
+// Encodes the maps for slot tensors of hist_planes (P * S) and z_planes (P * 4) planes of
+// nx x ny cells; false (with the reason) when the driver has no tensor-map encoder or refuses.
+bool encode_tile_maps(TileMaps* m, const DevGeo& g, const float* hist, int64_t hist_planes, const float* z,
+                      int64_t z_planes, const float* coef, std::string* why);
+void launch_fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream);
+void launch_adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream);
+constexpr int TILE_OWNED = 48;    // owned tile width and height of the tile kernels
+constexpr int TILE_MAX_FWD = 8;   // forward steps per tile launch at most
 
 }  // namespace tomo

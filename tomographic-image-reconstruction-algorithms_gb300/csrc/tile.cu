@@ -3,29 +3,39 @@
 // The warp-strip kernels (strip.cu) advance every group of a pass by one or two time steps per
 // launch.  On small grids (128 x 128, or one group of 512 x 512 in an ART pass) a step is too
 // little work to fill the GPU, and the time goes into the launches themselves.  These kernels
-// advance a 2-D tile by up to TMAX steps per launch: a block stages its 32 x 32 tile plus a halo
-// of 8 cells (48 x 48) of the two input slices, the coefficient, the sponge factor and the
-// receiver map in shared memory, then runs the steps there -- the computed region shrinks by
-// one cell per step, so the halo cells are computed redundantly and no block waits for another
-// inside a launch -- and writes every step's owned cells (the forward history, records,
-// checkpoints; the adjoint's last two slices and the correlation).
+// advance a 2-D tile by up to 8 steps per launch.  A block owns a 48 x 48 tile; the tile plus a
+// halo of 8 cells (a 64 x 64 region) of the two input slices, the coefficient, the sponge factor
+// and the receiver map arrive in shared memory as five TMA tile copies (cp.async.bulk.tensor,
+// zero-filled outside the grid) completing on one mbarrier.  The block then runs the steps with
+// the region's cells in registers: the computed region shrinks by one cell per step, so the halo
+// is computed redundantly and no block waits for another inside a launch.  Every step writes
+// the owned cells (the forward history, records and checkpoints; for the adjoint only the last
+// two slices and the correlation at the end).
 //
-// Work layout: a block of 32 warps; each warp computes whole rows of the region, a lane two
-// neighbouring cells (64-bit shared-memory accesses, west / east neighbours by shuffles).  Warp w
-// always computes the tile's row w (owned rows 8 .. 39 of the region), so a lane's owned cells
-// stay in its registers from step to step (the adjoint's correlation accumulates there); warps
-// 0 .. 13 also compute the 14 halo rows.  Each step computes rows 1 .. 46 and columns 0 .. 47 of
-// the region: cells outside the shrinking valid region produce values that only cells outside
-// it read, so no cell needs a branch.
+// Work layout: 16 warps; warp w holds region rows 4w .. 4w+3, lane l the columns 2l, 2l+1 of
+// each, so a thread keeps 8 cells (both input slices, coefficient and sponge factor) in
+// registers from step to step.  East / west neighbours come by warp shuffles, north / south
+// neighbours from the thread's own rows, and at the edges of a warp's band from the first and
+// last rows each warp publishes per step in a double-buffered exchange array (one barrier per
+// step).  A lane's two cells are evaluated in packed FP32x2 arithmetic with the operation order
+// and rounding of the cell.cuh helpers, so a sweep gives the strip kernels' bits (tested).  The
+// adjoint's correlation needs u(m-1) around the owned cells each step: one TMA copy per step
+// (rows 7 .. 56 of the region) into a three-slot ring, issued two steps ahead.
 //
-// Cells are evaluated with the helpers of cell.cuh in the strip kernels' operation order, so a
-// sweep gives the strip kernels' bits (tested).  Adjoint launches advance T in {1, 2, 6} steps:
-// the adjoint ring has four slots and these are the step counts whose two output slices never
-// fall on the two input slices' slots.
+// Adjoint launches advance T in {1, 2, 6} steps: the adjoint ring has four slots and these are
+// the step counts whose two output slices never fall on the two input slices' slots.  Forward
+// launches take T <= S - 2 so the slices they write never land on the slots they read.
+//
+// Waits: every mbarrier wait is bounded by TileWait::wait_ns of %globaltimer; a block whose copy
+// has not arrived by then records the failure in the host-visible error word, waits (again
+// bounded) for its other copies and returns; the host turns the word into TOMO_ERR_TIMEOUT.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
+#include <string>
 
 #include "internal.h"
 
@@ -34,300 +44,524 @@ namespace {
 
 #include "cell.cuh"
 
-constexpr int TW = 32;               // owned tile width and height
-constexpr int HALO = 8;              // staged halo (TMAX steps)
-constexpr int RW = TW + 2 * HALO;    // staged region: 48 x 48
-constexpr int RC = RW * RW;
-constexpr int TPB = 1024;            // 32 warps
-constexpr int UR = TW + 2;           // correlation's forward slice: rows 7 .. 40 of the region, pitch RW
-constexpr int UC = UR * RW;
+constexpr int TW = TILE_OWNED;       // owned tile width: 48 columns
+constexpr int HALO = 8;              // halo (steps per forward launch at most)
+constexpr int RX = TW + 2 * HALO;    // region width: 64 columns (32 lanes x 2 cells)
+constexpr int UOFF = HALO - 1;       // correlation slice: owned rows plus one above and below
+constexpr int TMAXF = TILE_MAX_FWD;
+static_assert(TMAXF <= HALO, "forward steps per launch exceed the halo");
+
+// Tile shapes: WARPS warps of 4 region rows, region RX x 4 WARPS, owned TW x (4 WARPS - 16).
+template <int WARPS>
+struct Shape {
+    static constexpr int TPB = 32 * WARPS;
+    static constexpr int RH = 4 * WARPS;                  // region rows
+    static constexpr int TH = RH - 2 * HALO;              // owned rows
+    static constexpr int RCH = RX * RH;
+    static constexpr int UROWS = TH + 2;
+    static constexpr uint32_t REGION_BYTES = 5u * RCH * 4u;
+    static constexpr uint32_t USLICE_BYTES = (uint32_t)UROWS * RX * 4u;
+    static constexpr int SET = WARPS == 16 ? 0 : 1;       // map set of encode_tile_maps
+    static constexpr int MINB = WARPS <= 10 ? 2 : 1;      // blocks per SM the launch bounds ask for
+};
+
+// Kernel-parameter copy of one shape's maps: slot tensor (region boxes), slot tensor
+// (correlation-slice boxes), adjoint ring, coefficient, sponge map, receiver map.
+struct TileTma {
+    CUtensorMap hist, histu, z, coef, dmap, rid;
+};
+static_assert(sizeof(TileTma) == sizeof(TileMaps::raw[0]), "tensor map size");
 
 __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+__device__ __forceinline__ uint32_t sm_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Rows a warp computes each step: its owned row 8 + w, and for warps 0 .. 13 one halo row
-// (1 .. 7, then 40 .. 46).
-__device__ __forceinline__ int halo_row(int w) { return w < 7 ? 1 + w : 33 + w; }
+// ---- mbarrier and TMA (PTX)
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(sm_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(sm_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(sm_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t gtimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+// Waits for phase `parity` of the barrier to complete, at most limit_ns; false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = gtimer();
+    do {
+        if (mbar_try_wait(bar, parity)) return true;
+    } while (gtimer() - t0 < limit_ns);
+    return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+            "r"(sm_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(sm_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(sm_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(sm_addr(bar))
+        : "memory");
+}
 
+// Forward cell update of a lane's two cells (fwd_cell of cell.cuh, packed).
+__device__ __forceinline__ float2 fwd_cell2(float2 e, float2 w, float2 s, float2 n, float2 u, float2 up, float2 c,
+                                            float2 d, float2 a) {
+    return pk_fma(d, pk_fma(c, lap5_2(e, w, s, n, u), pk_fma(make_float2(2.f, 2.f), u, make_float2(-up.x, -up.y))),
+                  a);
+}
+
+// Whether some row of warp w's band is still inside the valid region at step t (rows t .. RH-1-t).
+template <int RH>
+__device__ __forceinline__ bool band_live(int w, int t) {
+    return 4 * w + 3 >= t && 4 * w <= RH - 1 - t;
+}
+
+template <int WARPS>
 struct FwdSmem {
-    float a[RC], b[RC];   // u(m-1) and u(m-2), rotating (u(m) overwrites u(m-2) in place)
-    float c[RC];          // coefficient C^2 (1+f)
-    float d[RC];          // sponge factor
-    int rid[RC];          // receiver channel of the cell, -1 none
-    float em[RC];         // 1 where the cell emits for the block's group, else 0
+    using S = Shape<WARPS>;
+    float u1[S::RCH], u2[S::RCH], c[S::RCH], d[S::RCH];   // region: u(k0), u(k0-1), coefficient, sponge
+    int rid[S::RCH];                                      // receiver channel (0 outside the grid: masked)
+    float xch[2][WARPS][2][RX];                           // per step: each warp's first and last row
+    uint64_t bar;
 };
+template <int WARPS>
 struct AdjSmem {
-    float za[RC], zb[RC]; // z(m+1) and z(m+2), rotating (z(m) overwrites z(m+2) in place)
-    float pa[RC], pb[RC]; // products c z of the current z(m+1) and of the z(m) being computed
-    float c[RC];
-    float d[RC];
-    int rid[RC];
-    float u[3][UC];       // forward slices for the correlation (step t uses u[t % 3])
+    using S = Shape<WARPS>;
+    float z1[S::RCH], z2[S::RCH], c[S::RCH], d[S::RCH];   // region: z(kz0+1), z(kz0+2), coefficient, sponge
+    int rid[S::RCH];
+    float u[3][S::UROWS * RX];                            // correlation slices, step t in u[t % 3]
+    float xch[2][WARPS][2][RX];                           // per step: products c z of each warp's edge rows
+    uint64_t bar[4];                                      // region; u[0], u[1], u[2]
 };
 
-// Region cell (rx, ry) is grid cell (gx0 + rx, gy0 + ry).  The five arrays arrive by 16-byte
-// cp.async copies (a row of the region is 12 four-cell chunks; nx % 4 == 0, so a chunk is wholly
-// inside or outside the grid), zero-filled outside the grid: field 0 and coefficient 0 (cells
-// outside stay 0, or never reach an inside cell), sponge 0, receiver entry fixed to -1 after.
-constexpr int CHUNKS = RW / 4;      // 12
-__device__ __forceinline__ void stage_async(const DevGeo& g, const float* pa, const float* pb, const float* coef,
-                                            int gx0, int gy0, float* sa, float* sb, float* sc, float* sd, int* srid) {
+// Receiver / emitter bits of a thread's 8 cells (bit 2r + i: row r, column i of the pair) from
+// the staged receiver map, cells outside the grid excluded.
+__device__ __forceinline__ void cell_masks(const DevGeo& g, const int* rid, int gx0, int gy0, int ry0, int lane,
+                                           int ggl, unsigned& rmask, unsigned& emask) {
+    rmask = emask = 0u;
+    const int x = gx0 + 2 * lane;
 #pragma unroll
-    for (int arr = 0; arr < 5; ++arr) {
-        const float* src = arr == 0 ? pa : arr == 1 ? pb : arr == 2 ? coef : arr == 3 ? g.dmap
-                                                                       : reinterpret_cast<const float*>(g.rid);
-        float* dst = arr == 0 ? sa : arr == 1 ? sb : arr == 2 ? sc : arr == 3 ? sd : reinterpret_cast<float*>(srid);
-        for (int c = threadIdx.x; c < RW * CHUNKS; c += TPB) {
-            const int ry = c / CHUNKS, rx = 4 * (c % CHUNKS);
-            const int x = gx0 + rx, y = gy0 + ry;
-            const bool ok = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
-            cp_async16((unsigned)__cvta_generic_to_shared(dst + ry * RW + rx), ok ? src + (int64_t)y * g.nx + x : src,
-                       ok);
+    for (int r = 0; r < 4; ++r) {
+        const int y = gy0 + ry0 + r;
+        const int2 rv = *reinterpret_cast<const int2*>(rid + (ry0 + r) * RX + 2 * lane);
+        const bool iny = y >= 0 && y < g.ny;
+        if (iny && x >= 0 && x < g.nx && rv.x >= 0) {
+            rmask |= 1u << (2 * r);
+            if (rv.x / g.gs == ggl) emask |= 1u << (2 * r);
+        }
+        if (iny && x + 1 >= 0 && x + 1 < g.nx && rv.y >= 0) {
+            rmask |= 2u << (2 * r);
+            if (rv.y / g.gs == ggl) emask |= 2u << (2 * r);
         }
     }
 }
 
-__device__ __forceinline__ bool region_in_grid(const DevGeo& g, int gx0, int gy0, int idx) {
-    const int x = gx0 + idx % RW, y = gy0 + idx / RW;
-    return x >= 0 && x < g.nx && y >= 0 && y < g.ny;
-}
-
-// One forward row: cells (2 lane, 2 lane + 1) of region row ry from u(m-1) (cur) and u(m-2)
-// (prv, overwritten).  Lanes 24 .. 31 hold no cells but join the shuffles.
-__device__ __forceinline__ float2 fwd_row(const FwdSmem& sm, const float* cur, float* prv, int ry, int lane, float src) {
-    const bool act = lane < RW / 2;
-    const int s = ry * RW + 2 * lane;
-    const float2 zero = make_float2(0.f, 0.f);
-    const float2 uc = act ? lds2(cur + s) : zero;
-    const float w = __shfl_up_sync(FULL, uc.y, 1), e = __shfl_down_sync(FULL, uc.x, 1);
-    float2 v = zero;
-    if (act) {
-        const float2 us = lds2(cur + s - RW), un = lds2(cur + s + RW), up = lds2(prv + s);
-        const float2 c = lds2(sm.c + s), d = lds2(sm.d + s), em = lds2(sm.em + s);
-        v.x = fwd_cell(uc.y, w, us.x, un.x, uc.x, up.x, c.x, d.x, em.x != 0.f ? src : 0.f);
-        v.y = fwd_cell(e, uc.x, us.y, un.y, uc.y, up.y, c.y, d.y, em.y != 0.f ? src : 0.f);
-        sts2(prv + s, v);
-    }
-    return v;
-}
-
-constexpr int TMAXF = 8;   // forward steps per launch at most
-
-__global__ void __launch_bounds__(TPB) k_fwd_tile(DevGeo g, const float* __restrict__ coef, TileFwd a,
-                                                  int tiles_x) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    FwdSmem& sm = *reinterpret_cast<FwdSmem*>(smraw);
+template <int WARPS>
+__global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
+    k_fwd_tile(DevGeo g, const __grid_constant__ TileTma tm, TileFwd a, int tiles_x) {
+    using S = Shape<WARPS>;
+    constexpr int RH = S::RH, TH = S::TH;
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    FwdSmem<WARPS>& sm = *reinterpret_cast<FwdSmem<WARPS>*>(smraw);
     const int gl = blockIdx.y;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    const int gx0 = tx * TW - HALO, gy0 = ty * TW - HALO;
+    const int gx0 = tx * TW - HALO, gy0 = ty * TH - HALO;
     const int64_t N = (int64_t)g.nx * g.ny;
-    float* base = a.hist + gl * a.gstride;
-    const int ggl = a.g0 + gl;                     // global group index
-    stage_async(g, base + (int64_t)(a.k0 % a.S) * N, base + (int64_t)((a.k0 - 1) % a.S) * N, coef, gx0, gy0, sm.a,
-                sm.b, sm.c, sm.d, sm.rid);
-    cp_async_commit();
-    // the source amplitude of each step, read while the copies fly
-    float srcv[TMAXF];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int ggl = a.g0 + gl;
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    // source amplitudes and measured record rows of the launch's steps, loaded while the copies fly
+    // (no global load stays on a step's critical path)
+    float* const ssrc = reinterpret_cast<float*>(smraw + sizeof(FwdSmem<WARPS>));   // [TMAXF]
+    float* const smeas = ssrc + TMAXF;                                              // [T][nch]
+    if (threadIdx.x < TMAXF) {
+        const int k = a.k0 + threadIdx.x;          // step threadIdx.x + 1 computes slice k + 1
+        ssrc[threadIdx.x] = (int)threadIdx.x < a.T && k < g.n_src_steps ? g.src[k] : 0.f;
+    }
+    if (a.gmeas) {
+        const float* gm = a.gmeas + ((int64_t)gl * g.nt + a.k0 + 1) * g.nch;
+        for (int i = threadIdx.x; i < a.T * g.nch; i += S::TPB) smeas[i] = gm[i];
+    }
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&sm.bar, S::REGION_BYTES + a.w.extra_tx);
+        tma_load_3d(sm.u1, &tm.hist, gx0, gy0, gl * a.S + a.k0 % a.S, &sm.bar);
+        tma_load_3d(sm.u2, &tm.hist, gx0, gy0, gl * a.S + (a.k0 - 1) % a.S, &sm.bar);
+        tma_load_2d(sm.c, &tm.coef, gx0, gy0, &sm.bar);
+        tma_load_2d(sm.d, &tm.dmap, gx0, gy0, &sm.bar);
+        tma_load_2d(sm.rid, &tm.rid, gx0, gy0, &sm.bar);
+    }
+    if (!__syncthreads_and(mbar_wait(&sm.bar, 0, a.w.wait_ns))) {
+        if (threadIdx.x == 0) atomicOr(a.w.err, 1u);
+        mbar_wait(&sm.bar, 0, a.w.wait_ns);
+        return;
+    }
+    const int ry0 = 4 * w;
+    float2 ua[4], ub[4], cc[4], dd[4];   // ua = u(k0), ub = u(k0-1); then alternately overwritten
 #pragma unroll
-    for (int t = 0; t < TMAXF; ++t) {
-        const int k = a.k0 + t;                    // step t+1 computes slice k+1
-        srcv[t] = (t < a.T && k < g.n_src_steps) ? g.src[k] : 0.f;
+    for (int r = 0; r < 4; ++r) {
+        const int s = (ry0 + r) * RX + 2 * lane;
+        ua[r] = lds2(sm.u1 + s);
+        ub[r] = lds2(sm.u2 + s);
+        cc[r] = lds2(sm.c + s);
+        dd[r] = lds2(sm.d + s);
     }
-    cp_async_wait<0>();
-    __syncthreads();
-    // receiver entries outside the grid, and the emitter flags (channel = transducer; its group =
-    // transducer / group size)
-    for (int idx = threadIdx.x; idx < RC; idx += TPB) {
-        int r = sm.rid[idx];
-        if (!region_in_grid(g, gx0, gy0, idx)) sm.rid[idx] = r = -1;
-        sm.em[idx] = (r >= 0 && r / g.gs == ggl) ? 1.f : 0.f;
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned rmask, emask;
+    cell_masks(g, sm.rid, gx0, gy0, ry0, lane, ggl, rmask, emask);
+    // owned cells: rows 8 .. RH-9 (warps 2 .. WARPS-3), columns 8 .. 55 (lanes 4 .. 27), inside the grid
+    const int ox = gx0 + 2 * lane;
+    const bool own = w >= HALO / 4 && w < WARPS - HALO / 4 && lane >= HALO / 2 && lane < (HALO + TW) / 2 && ox < g.nx;
+    if (!own) rmask = 0u;
     const bool noisy = a.gmeas && g.noise_key;
     const uint64_t key = noisy ? *g.noise_key : 0;
-    // owned cells of this lane: row 8 + warp, columns 2 lane, 2 lane + 1 for lanes 4 .. 19
-    const int orow = HALO + warp;
-    const int ox = gx0 + 2 * lane, oy = gy0 + orow;
-    const bool own = lane >= HALO / 2 && lane < (HALO + TW) / 2 && ox < g.nx && oy < g.ny;
-    const int64_t oq = (int64_t)oy * g.nx + ox;
-    const int2 orid = own ? *reinterpret_cast<const int2*>(sm.rid + orow * RW + 2 * lane) : make_int2(-1, -1);
-    const int hrow = warp < 14 ? halo_row(warp) : -1;
-    float* cur = sm.a;   // u(m-1)
-    float* prv = sm.b;   // u(m-2), overwritten in place by u(m)
+    float* const obase = a.hist + gl * a.gstride + (int64_t)(gy0 + ry0) * g.nx + ox;   // owned row 0 of slot 0
+    float* const cbase = a.ckpt ? a.ckpt + gl * a.ckstride + (int64_t)(gy0 + ry0) * g.nx + ox : nullptr;
+    const int orows = own ? min(4, g.ny - (gy0 + ry0)) : 0;   // owned rows of this thread inside the grid
     int slot = (a.k0 + 1) % a.S;                   // slot of slice m
     int mk = a.ckpt ? (a.k0 + 1) % a.K : -1;       // m mod K
-#pragma unroll 1
-    for (int t = 1; t <= a.T; ++t) {
+    const float2 zero = make_float2(0.f, 0.f);
+    // one step: u(m) from cur = u(m-1) and prv = u(m-2), written over prv
+    auto step = [&](float2 (&cur)[4], float2 (&prv)[4], int t) {
         const int m = a.k0 + t;                    // slice computed
-        float src = 0.f;
+        const float src = ssrc[t - 1];
+        // the rows below and above the band, u(m-1)
+        float2 sb, nb;
+        if (t == 1) {
+            sb = w > 0 ? lds2(sm.u1 + (ry0 - 1) * RX + 2 * lane) : zero;
+            nb = w < WARPS - 1 ? lds2(sm.u1 + (ry0 + 4) * RX + 2 * lane) : zero;
+        } else {
+            const float* xb = &sm.xch[(t - 1) & 1][0][0][0];
+            sb = w > 0 ? lds2(xb + ((w - 1) * 2 + 1) * RX + 2 * lane) : zero;
+            nb = w < WARPS - 1 ? lds2(xb + ((w + 1) * 2) * RX + 2 * lane) : zero;
+        }
+        if (band_live<RH>(w, t)) {
 #pragma unroll
-        for (int j = 0; j < TMAXF; ++j) src = j == t - 1 ? srcv[j] : src;
-        const float2 v = fwd_row(sm, cur, prv, orow, lane, src);
-        if (hrow >= 0) fwd_row(sm, cur, prv, hrow, lane, src);
-        if (own) {
-            *reinterpret_cast<float2*>(base + (int64_t)slot * N + oq) = v;
-            if (mk == 0 || mk == 1) {
-                // checkpoint: chunk ch >= 1 keeps slices ch K - 1 (which 1 ... ) as engine.cu ck_of
-                const int ch = mk == 0 ? m / a.K : (m - 1) / a.K, which = mk == 0 ? 0 : 1;
-                if (ch >= 1 && ch < a.nchunk)
-                    *reinterpret_cast<float2*>(a.ckpt + gl * a.ckstride + ((int64_t)ch * 2 + which) * N + oq) = v;
+            for (int r = 0; r < 4; ++r) {
+                const float2 u = cur[r];
+                const float wv = __shfl_up_sync(FULL, u.y, 1), ev = __shfl_down_sync(FULL, u.x, 1);
+                const float2 s = r == 0 ? sb : cur[r - 1], n = r == 3 ? nb : cur[r + 1];
+                const float2 am = make_float2((emask >> (2 * r)) & 1u ? src : 0.f, (emask >> (2 * r)) & 2u ? src : 0.f);
+                prv[r] = fwd_cell2(make_float2(u.y, ev), make_float2(wv, u.x), s, n, u, prv[r], cc[r], dd[r], am);
             }
-            if ((orid.x >= 0 || orid.y >= 0) && a.gout) {
-                const int64_t gbase = ((int64_t)gl * g.nt + m) * g.nch;
-                if (orid.x >= 0) {
-                    const float vv = noisy ? v.x * noise_factor(key, g.noise_level, ggl, m, orid.x) : v.x;
-                    a.gout[gbase + orid.x] = a.gmeas ? a.gmeas[gbase + orid.x] - vv : vv;
-                }
-                if (orid.y >= 0) {
-                    const float vv = noisy ? v.y * noise_factor(key, g.noise_level, ggl, m, orid.y) : v.y;
-                    a.gout[gbase + orid.y] = a.gmeas ? a.gmeas[gbase + orid.y] - vv : vv;
+            sts2(&sm.xch[t & 1][w][0][2 * lane], prv[0]);
+            sts2(&sm.xch[t & 1][w][1][2 * lane], prv[3]);
+            if (orows > 0) {
+                float* const os = obase + (int64_t)slot * N;
+                // checkpoint: chunk ch >= 1 keeps slices ch K - 1 (which 1) and ch K (which 0)
+                const int ch = mk == 0 ? m / a.K : mk == 1 ? (m - 1) / a.K : -1, which = mk == 0 ? 0 : 1;
+                float* const ck = (ch >= 1 && ch < a.nchunk) ? cbase + ((int64_t)ch * 2 + which) * N : nullptr;
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    if (r >= orows) break;
+                    *reinterpret_cast<float2*>(os + (int64_t)r * g.nx) = prv[r];
+                    if (ck) *reinterpret_cast<float2*>(ck + (int64_t)r * g.nx) = prv[r];
+                    const unsigned rb = (rmask >> (2 * r)) & 3u;
+                    if (rb && a.gout) {
+                        const int2 rv = *reinterpret_cast<const int2*>(sm.rid + (ry0 + r) * RX + 2 * lane);
+                        const int64_t gbase = ((int64_t)gl * g.nt + m) * g.nch;
+                        const float* sme = smeas + (t - 1) * g.nch;
+                        if (rb & 1u) {
+                            const float vv = noisy ? prv[r].x * noise_factor(key, g.noise_level, ggl, m, rv.x) : prv[r].x;
+                            a.gout[gbase + rv.x] = a.gmeas ? sme[rv.x] - vv : vv;
+                        }
+                        if (rb & 2u) {
+                            const float vv = noisy ? prv[r].y * noise_factor(key, g.noise_level, ggl, m, rv.y) : prv[r].y;
+                            a.gout[gbase + rv.y] = a.gmeas ? sme[rv.y] - vv : vv;
+                        }
+                    }
                 }
             }
         }
         slot = slot + 1 == a.S ? 0 : slot + 1;
         if (mk >= 0) mk = mk + 1 == a.K ? 0 : mk + 1;
         __syncthreads();
-        float* tmp = cur;
-        cur = prv;
-        prv = tmp;
+    };
+#pragma unroll 1
+    for (int t = 1; t <= a.T; t += 2) {
+        step(ua, ub, t);                           // u(k0+t) into ub
+        if (t + 1 <= a.T) step(ub, ua, t + 1);     // u(k0+t+1) into ua
     }
 }
 
-// Issues the correlation's forward slice as cp.async copies: rows 7 .. 40 (owned rows plus one)
-// and the chunks of columns 4 .. 43 of the region, pitch RW, zero-filled outside the grid.
-constexpr int UCH = 10;             // four-cell chunks of a staged row (columns 4 .. 43)
-__device__ __forceinline__ void stage_u_async(const DevGeo& g, const float* __restrict__ u, int gx0, int gy0,
-                                              float* __restrict__ dst) {
-    const int c = threadIdx.x;
-    if (c < UR * UCH) {
-        const int cy = c / UCH, cx = 4 + 4 * (c % UCH);
-        const int x = gx0 + cx, y = gy0 + HALO - 1 + cy;
-        const bool ok = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
-        cp_async16((unsigned)__cvta_generic_to_shared(dst + cy * RW + cx), ok ? u + (int64_t)y * g.nx + x : u, ok);
-    }
+// Issues the correlation slice of step t (u(kz0 - t), region rows 7 .. 8+TH) into u[t % 3].
+template <int WARPS>
+__device__ __forceinline__ void issue_u(AdjSmem<WARPS>& sm, const TileTma& tm, const TileAdj& a, int gl, int gx0,
+                                        int gy0, int t) {
+    uint64_t* bar = &sm.bar[1 + t % 3];
+    mbar_expect_tx(bar, Shape<WARPS>::USLICE_BYTES);
+    tma_load_3d(sm.u[t % 3], &tm.histu, gx0, gy0 + UOFF, gl * a.S + (a.kz0 - t) % a.S, bar);
 }
+// Parity of the u[t % 3] barrier phase that step t waits for (its (t-1)/3-th use).
+__device__ __forceinline__ uint32_t u_parity(int t) { return (uint32_t)((t - 1) / 3) & 1u; }
 
-// One adjoint row: z(m) at cells (2 lane, 2 lane + 1) of region row ry from z(m+1) (z1, with its
-// products p1) and z(m+2) (z2, overwritten); writes the products c z(m) to p2.
-__device__ __forceinline__ float2 adj_row(const AdjSmem& sm, const float* z1, float* z2, const float* p1, float* p2,
-                                          int ry, int lane, const float* __restrict__ rrm) {
-    const bool act = lane < RW / 2;
-    const int s = ry * RW + 2 * lane;
-    const float2 zero = make_float2(0.f, 0.f);
-    const float2 p0 = act ? lds2(p1 + s) : zero;
-    const float pw = __shfl_up_sync(FULL, p0.y, 1), pe = __shfl_down_sync(FULL, p0.x, 1);
-    float2 v = zero;
-    if (act) {
-        const float2 ps = lds2(p1 + s - RW), pn = lds2(p1 + s + RW);
-        const float2 z = lds2(z1 + s), zz = lds2(z2 + s), c = lds2(sm.c + s), d = lds2(sm.d + s);
-        const int2 r = *reinterpret_cast<const int2*>(sm.rid + s);
-        const float ix = r.x >= 0 ? rrm[r.x] : 0.f, iy = r.y >= 0 ? rrm[r.y] : 0.f;
-        v.x = adj_cell(p0.y, pw, ps.x, pn.x, p0.x, z.x, zz.x, ix, d.x);
-        v.y = adj_cell(pe, p0.x, ps.y, pn.y, p0.y, z.y, zz.y, iy, d.y);
-        sts2(z2 + s, v);
-        sts2(p2 + s, make_float2(mul(c.x, v.x), mul(c.y, v.y)));
-    }
-    return v;
-}
-
-__global__ void __launch_bounds__(TPB) k_adj_tile(DevGeo g, const float* __restrict__ coef, TileAdj a,
-                                                  int tiles_x) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    AdjSmem& sm = *reinterpret_cast<AdjSmem*>(smraw);
+template <int WARPS>
+__global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
+    k_adj_tile(DevGeo g, const __grid_constant__ TileTma tm, TileAdj a, int tiles_x) {
+    using S = Shape<WARPS>;
+    constexpr int RH = S::RH, TH = S::TH;
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    AdjSmem<WARPS>& sm = *reinterpret_cast<AdjSmem<WARPS>*>(smraw);
     const int gl = blockIdx.y;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    const int gx0 = tx * TW - HALO, gy0 = ty * TW - HALO;
+    const int gx0 = tx * TW - HALO, gy0 = ty * TH - HALO;
     const int64_t N = (int64_t)g.nx * g.ny;
-    float* zbase = a.z + gl * a.zstride;
-    const float* ub = a.hist + gl * a.ustride;
-    const float* rr = a.rr + gl * a.rrstride;
-    // copy groups: the region, then the forward slices of steps 1 and 2 (step t reads slice kz0 - t,
-    // u[t % 3]); every step then issues step t+2's slice and waits for its own, one group behind
-    stage_async(g, zbase + (int64_t)((a.kz0 + 1) & 3) * N, zbase + (int64_t)((a.kz0 + 2) & 3) * N, coef, gx0, gy0,
-                sm.za, sm.zb, sm.c, sm.d, sm.rid);
-    cp_async_commit();
-    int us = (a.kz0 - 1) % a.S;                    // slot of the slice step 1 reads
-    stage_u_async(g, ub + (int64_t)us * N, gx0, gy0, sm.u[1]);
-    cp_async_commit();
-    int un = us == 0 ? a.S - 1 : us - 1;           // slot of the next slice to issue (step 2's)
-    if (a.T >= 2) stage_u_async(g, ub + (int64_t)un * N, gx0, gy0, sm.u[2]);
-    cp_async_commit();
-    un = un == 0 ? a.S - 1 : un - 1;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int orow = HALO + warp;
-    const int ox = gx0 + 2 * lane, oy = gy0 + orow;
-    const bool own = lane >= HALO / 2 && lane < (HALO + TW) / 2 && ox < g.nx && oy < g.ny;
-    const int64_t oq = (int64_t)oy * g.nx + ox;
-    float2 cr = own ? *reinterpret_cast<const float2*>(a.corr + gl * a.cstride + oq) : make_float2(0.f, 0.f);
-    const int hrow = warp < 14 ? halo_row(warp) : -1;
-    cp_async_wait<2>();                            // the region
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x < 4) mbar_init(&sm.bar[threadIdx.x], 1);
+    if (threadIdx.x == 0) mbar_fence_init();
     __syncthreads();
-    // receiver entries outside the grid, and the products c z(kz0+1)
-    for (int idx = threadIdx.x; idx < RC; idx += TPB) {
-        if (!region_in_grid(g, gx0, gy0, idx)) sm.rid[idx] = -1;
-        sm.pa[idx] = mul(sm.c[idx], sm.za[idx]);
+    // residual rows of the launch's steps (z(m) injects rr[m]; row j holds m = kz0-T+1+j), loaded
+    // while the copies fly
+    float* const srr = reinterpret_cast<float*>(smraw + sizeof(AdjSmem<WARPS>));   // [T][nch]
+    {
+        const float* rg = a.rr + gl * a.rrstride + (int64_t)(a.kz0 - a.T + 1) * g.nch;
+        for (int i = threadIdx.x; i < a.T * g.nch; i += S::TPB) srr[i] = rg[i];
     }
-    float* z1 = sm.za;   // z(m+1)
-    float* z2 = sm.zb;   // z(m+2), overwritten in place by z(m)
-    float* p1 = sm.pa;   // c z(m+1)
-    float* p2 = sm.pb;   // c z(m)
-    float2 zl = make_float2(0.f, 0.f), zp = zl;   // this lane's owned z(m) and z(m+1)
-#pragma unroll 1
-    for (int t = 1; t <= a.T; ++t) {
-        const int m = a.kz0 - t + 1;
-        const float* rrm = rr + (int64_t)m * g.nch;
-        cp_async_wait<1>();                        // this thread's copies of u[t % 3] are done ...
-        __syncthreads();                           // ... and every thread's; step t-1 is complete
-        const float2 v = adj_row(sm, z1, z2, p1, p2, orow, lane, rrm);
-        if (hrow >= 0) adj_row(sm, z1, z2, p1, p2, hrow, lane, rrm);
-        // the correlation of the owned cells with the Laplacian of u(m-1), in registers
-        const float* usl = sm.u[t % 3] + (orow - (HALO - 1)) * RW + 2 * lane;
-        const bool act = lane < RW / 2;
-        const float2 u0 = act ? lds2(usl) : make_float2(0.f, 0.f);
-        const float uw = __shfl_up_sync(FULL, u0.y, 1), ue = __shfl_down_sync(FULL, u0.x, 1);
-        if (own) {
-            const float2 usn = lds2(usl - RW), unn = lds2(usl + RW);
-            cr.x = __fmaf_rn(v.x, lap5(u0.y, uw, usn.x, unn.x, u0.x), cr.x);
-            cr.y = __fmaf_rn(v.y, lap5(ue, u0.x, usn.y, unn.y, u0.y), cr.y);
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&sm.bar[0], S::REGION_BYTES + a.w.extra_tx);
+        tma_load_3d(sm.z1, &tm.z, gx0, gy0, gl * 4 + ((a.kz0 + 1) & 3), &sm.bar[0]);
+        tma_load_3d(sm.z2, &tm.z, gx0, gy0, gl * 4 + ((a.kz0 + 2) & 3), &sm.bar[0]);
+        tma_load_2d(sm.c, &tm.coef, gx0, gy0, &sm.bar[0]);
+        tma_load_2d(sm.d, &tm.dmap, gx0, gy0, &sm.bar[0]);
+        tma_load_2d(sm.rid, &tm.rid, gx0, gy0, &sm.bar[0]);
+        issue_u(sm, tm, a, gl, gx0, gy0, 1);
+        if (a.T >= 2) issue_u(sm, tm, a, gl, gx0, gy0, 2);
+    }
+    const int ry0 = 4 * w;
+    const int ox = gx0 + 2 * lane;
+    const bool own_rows = w >= HALO / 4 && w < WARPS - HALO / 4;
+    const bool own = own_rows && lane >= HALO / 2 && lane < (HALO + TW) / 2 && ox < g.nx;
+    const int orows = own ? min(4, g.ny - (gy0 + ry0)) : 0;
+    float* const cbase = a.corr + gl * a.cstride + (int64_t)(gy0 + ry0) * g.nx + ox;
+    float2 cr[4];
+    const float2 zero = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) cr[r] = r < orows ? *reinterpret_cast<const float2*>(cbase + (int64_t)r * g.nx) : zero;
+    if (!__syncthreads_and(mbar_wait(&sm.bar[0], 0, a.w.wait_ns))) {
+        if (threadIdx.x == 0) atomicOr(a.w.err, 1u);
+        for (int s = 1; s <= a.T && s <= 2; ++s) mbar_wait(&sm.bar[1 + s % 3], u_parity(s), a.w.wait_ns);
+        return;
+    }
+    // za = z(kz0+1), zb = z(kz0+2), pa = c z(kz0+1); then alternately overwritten
+    float2 za[4], zb[4], cc[4], dd[4], pa[4], pb[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int s = (ry0 + r) * RX + 2 * lane;
+        za[r] = lds2(sm.z1 + s);
+        zb[r] = lds2(sm.z2 + s);
+        cc[r] = lds2(sm.c + s);
+        dd[r] = lds2(sm.d + s);
+        pa[r] = pk_mul(cc[r], za[r]);
+    }
+    unsigned rmask, emask;
+    cell_masks(g, sm.rid, gx0, gy0, ry0, lane, 0, rmask, emask);
+    // one step: z(m) from zc = z(m+1) (products pc) and zp = z(m+2), written over zp, its
+    // products over pn; false when a copy wait timed out (the launch is abandoned)
+    auto step = [&](float2 (&zc)[4], float2 (&zp)[4], float2 (&pc)[4], float2 (&pn)[4], int t) -> bool {
+        const float* rrm = srr + (a.T - t) * g.nch;   // rr[m] of the slice computed, z(m), m = kz0-t+1
+        // warp-uniform, so the shuffles below run with every lane of the warp
+        const bool ok = __all_sync(FULL, mbar_wait(&sm.bar[1 + t % 3], u_parity(t), a.w.wait_ns));
+        // products c z(m+1) of the rows below and above the band
+        float2 sb, nb;
+        if (t == 1) {
+            sb = w > 0 ? pk_mul(lds2(sm.c + (ry0 - 1) * RX + 2 * lane), lds2(sm.z1 + (ry0 - 1) * RX + 2 * lane)) : zero;
+            nb = w < WARPS - 1 ? pk_mul(lds2(sm.c + (ry0 + 4) * RX + 2 * lane), lds2(sm.z1 + (ry0 + 4) * RX + 2 * lane))
+                               : zero;
+        } else {
+            const float* xb = &sm.xch[(t - 1) & 1][0][0][0];
+            sb = w > 0 ? lds2(xb + ((w - 1) * 2 + 1) * RX + 2 * lane) : zero;
+            nb = w < WARPS - 1 ? lds2(xb + ((w + 1) * 2) * RX + 2 * lane) : zero;
         }
-        zp = zl;
-        zl = v;
+        if (ok && band_live<RH>(w, t)) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float2 p = pc[r];
+                const float pw = __shfl_up_sync(FULL, p.y, 1), pe = __shfl_down_sync(FULL, p.x, 1);
+                const float2 ps = r == 0 ? sb : pc[r - 1], pnb = r == 3 ? nb : pc[r + 1];
+                float2 inj = zero;
+                const unsigned rb = (rmask >> (2 * r)) & 3u;
+                if (rb) {
+                    const int2 rv = *reinterpret_cast<const int2*>(sm.rid + (ry0 + r) * RX + 2 * lane);
+                    if (rb & 1u) inj.x = rrm[rv.x];
+                    if (rb & 2u) inj.y = rrm[rv.y];
+                }
+                zp[r] = adj_cell2(make_float2(p.y, pe), make_float2(pw, p.x), ps, pnb, p, zc[r], zp[r], inj, dd[r]);
+                pn[r] = pk_mul(cc[r], zp[r]);
+            }
+            if (own_rows) {
+                // correlation with the Laplacian of u(m-1) (rows ry0-1 .. ry0+4 of the region)
+                const float* ub = sm.u[t % 3] + (ry0 - UOFF) * RX + 2 * lane;
+                float2 ur[6];
+#pragma unroll
+                for (int i = 0; i < 6; ++i) ur[i] = lds2(ub + (i - 1) * RX);
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const float2 u = ur[r + 1];
+                    const float uw = __shfl_up_sync(FULL, u.y, 1), ue = __shfl_down_sync(FULL, u.x, 1);
+                    cr[r] = pk_fma(zp[r], lap5_2(make_float2(u.y, ue), make_float2(uw, u.x), ur[r], ur[r + 2], u), cr[r]);
+                }
+            }
+            sts2(&sm.xch[t & 1][w][0][2 * lane], pn[0]);
+            sts2(&sm.xch[t & 1][w][1][2 * lane], pn[3]);
+        }
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) atomicOr(a.w.err, 1u);
+            for (int s = t; s <= a.T && s <= t + 1; ++s) mbar_wait(&sm.bar[1 + s % 3], u_parity(s), a.w.wait_ns);
+            return false;
+        }
         // step t+2's slice into u[(t+2) % 3], last read by step t-1 (complete at the barrier above)
-        if (t + 2 <= a.T) {
-            stage_u_async(g, ub + (int64_t)un * N, gx0, gy0, sm.u[(t + 2) % 3]);
-            un = un == 0 ? a.S - 1 : un - 1;
-        }
-        cp_async_commit();
-        float* tmp = z1; z1 = z2; z2 = tmp;
-        tmp = p1; p1 = p2; p2 = tmp;
+        if (threadIdx.x == 0 && t + 2 <= a.T) issue_u(sm, tm, a, gl, gx0, gy0, t + 2);
+        return true;
+    };
+#pragma unroll 1
+    for (int t = 1; t <= a.T; t += 2) {
+        if (!step(za, zb, pa, pb, t)) return;                        // z(kz0-t+1) into zb
+        if (t + 1 <= a.T && !step(zb, za, pb, pa, t + 1)) return;    // z(kz0-t) into za
     }
-    cp_async_wait<0>();
     // z(kz0-T+1) and z(kz0-T+2) go to the ring (T = 1: only the first), with the correlation
-    if (own) {
+    if (orows > 0) {
+        const bool odd = a.T & 1;                  // odd T: the last slice is in zb
+        float* zbase = a.z + gl * a.zstride + (int64_t)(gy0 + ry0) * g.nx + ox;
         const int mlast = a.kz0 - a.T + 1;
-        *reinterpret_cast<float2*>(zbase + (int64_t)(mlast & 3) * N + oq) = zl;
-        if (a.T > 1) *reinterpret_cast<float2*>(zbase + (int64_t)((mlast + 1) & 3) * N + oq) = zp;
-        *reinterpret_cast<float2*>(a.corr + gl * a.cstride + oq) = cr;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if (r >= orows) break;
+            const int64_t o = (int64_t)r * g.nx;
+            *reinterpret_cast<float2*>(zbase + (int64_t)(mlast & 3) * N + o) = odd ? zb[r] : za[r];
+            if (a.T > 1) *reinterpret_cast<float2*>(zbase + (int64_t)((mlast + 1) & 3) * N + o) = odd ? za[r] : zb[r];
+            *reinterpret_cast<float2*>(cbase + o) = cr[r];
+        }
     }
+}
+
+// ---- host: tensor-map encoding (driver entry point, no link against libcuda)
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+    static const EncodeTiled fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<EncodeTiled>(p);
+    }();
+    return fn;
+}
+
+// One map over nx x ny (x planes) cells of 4 bytes, boxes of bx x by (x 1) cells, zero fill
+// outside the tensor.
+bool encode(EncodeTiled fn, unsigned char* out, CUtensorMapDataType type, const void* base, const DevGeo& g,
+            int64_t planes, int bx, int by, std::string* why, const char* what) {
+    CUtensorMap m;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)(planes > 0 ? planes : 1)};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.nx * 4u, (cuuint64_t)g.nx * (cuuint64_t)g.ny * 4u};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1u};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    const CUresult r = fn(&m, type, planes > 0 ? 3u : 2u, const_cast<void*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        if (why) *why = std::string("cuTensorMapEncodeTiled refused the ") + what + " map (" + std::to_string((int)r) + ")";
+        return false;
+    }
+    std::memcpy(out, &m, sizeof m);
+    return true;
 }
 
 }  // namespace
 
 bool tile_supported(const DevGeo& g, int profile) {
-    return profile == TOMO_PROFILE_CFG && g.rid != nullptr && g.dmap != nullptr && g.nx % 4 == 0;
+    // nx % 4 == 0: 16-byte row strides and tile origins (multiples of 4 cells) for the TMA copies;
+    // nch <= 2048: a launch's record rows (8 x nch floats) fit in shared memory next to the region
+    return profile == TOMO_PROFILE_CFG && g.rid != nullptr && g.dmap != nullptr && g.nx % 4 == 0 && g.nch <= 2048;
 }
 
-void launch_fwd_tile(const DevGeo& g, const float* coef, const TileFwd& a, void* stream) {
-    const int tiles_x = (g.nx + TW - 1) / TW, tiles_y = (g.ny + TW - 1) / TW;
-    cudaFuncSetAttribute(k_fwd_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FwdSmem));
-    k_fwd_tile<<<dim3(tiles_x * tiles_y, a.ng), TPB, sizeof(FwdSmem), (cudaStream_t)stream>>>(g, coef, a, tiles_x);
+bool encode_tile_maps(TileMaps* m, const DevGeo& g, const float* hist, int64_t hist_planes, const float* z,
+                      int64_t z_planes, const float* coef, std::string* why) {
+    m->ok = false;
+    if (!tile_supported(g, TOMO_PROFILE_CFG)) return false;
+    const EncodeTiled fn = encoder();
+    if (!fn) {
+        if (why) *why = "no cuTensorMapEncodeTiled entry point";
+        return false;
+    }
+    bool ok = true;
+    for (int set = 0; set < 2 && ok; ++set) {
+        const int rh = set == 0 ? Shape<16>::RH : Shape<10>::RH, ur = set == 0 ? Shape<16>::UROWS : Shape<10>::UROWS;
+        unsigned char(*r)[128] = m->raw[set];
+        ok = encode(fn, r[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, hist, g, hist_planes, RX, rh, why, "slot") &&
+             encode(fn, r[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, hist, g, hist_planes, RX, ur, why, "correlation slice") &&
+             encode(fn, r[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, z, g, z_planes, RX, rh, why, "adjoint ring") &&
+             encode(fn, r[3], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, coef, g, 0, RX, rh, why, "coefficient") &&
+             encode(fn, r[4], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, g.dmap, g, 0, RX, rh, why, "sponge") &&
+             encode(fn, r[5], CU_TENSOR_MAP_DATA_TYPE_INT32, g.rid, g, 0, RX, rh, why, "receiver");
+    }
+    m->ok = ok;
+    return ok;
 }
 
-void launch_adj_tile(const DevGeo& g, const float* coef, const TileAdj& a, void* stream) {
-    const int tiles_x = (g.nx + TW - 1) / TW, tiles_y = (g.ny + TW - 1) / TW;
-    cudaFuncSetAttribute(k_adj_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AdjSmem));
-    k_adj_tile<<<dim3(tiles_x * tiles_y, a.ng), TPB, sizeof(AdjSmem), (cudaStream_t)stream>>>(g, coef, a, tiles_x);
+namespace {
+template <int WARPS>
+void fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream) {
+    using S = Shape<WARPS>;
+    const int tiles_x = (g.nx + TW - 1) / TW, tiles_y = (g.ny + S::TH - 1) / S::TH;
+    TileTma tm;
+    std::memcpy(&tm, m.raw[S::SET], sizeof tm);
+    const size_t smem = sizeof(FwdSmem<WARPS>) + 4 * (TMAXF + (a.gmeas ? (size_t)a.T * g.nch : 0));
+    cudaFuncSetAttribute(k_fwd_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_fwd_tile<WARPS><<<dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, (cudaStream_t)stream>>>(g, tm, a, tiles_x);
+}
+template <int WARPS>
+void adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream) {
+    using S = Shape<WARPS>;
+    const int tiles_x = (g.nx + TW - 1) / TW, tiles_y = (g.ny + S::TH - 1) / S::TH;
+    TileTma tm;
+    std::memcpy(&tm, m.raw[S::SET], sizeof tm);
+    const size_t smem = sizeof(AdjSmem<WARPS>) + 4 * (size_t)a.T * g.nch;
+    cudaFuncSetAttribute(k_adj_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_adj_tile<WARPS><<<dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, (cudaStream_t)stream>>>(g, tm, a, tiles_x);
+}
+}  // namespace
+
+void launch_fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream) {
+    if (a.warps == 10) fwd_tile<10>(g, m, a, stream);
+    else fwd_tile<16>(g, m, a, stream);
+}
+
+void launch_adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream) {
+    if (a.warps == 10) adj_tile<10>(g, m, a, stream);
+    else adj_tile<16>(g, m, a, stream);
 }
 
 }  // namespace tomo
