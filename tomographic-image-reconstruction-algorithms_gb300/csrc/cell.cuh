@@ -149,3 +149,42 @@ __device__ __forceinline__ void cp_async16(unsigned smem_addr, const float* gmem
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// Programmatic dependent launch: a kernel launched by launch_pdl may start while the kernel
+// before it in the stream finishes.  Such a kernel reads nothing another kernel writes before
+// grid_dep_wait() (which returns once the previous kernel has completed and its writes are
+// visible; at once for a plain launch), then lets the next launch start early.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+// Launch that may overlap the end of the previous kernel in the stream (programmatic stream
+// serialization); TOMO_NO_PDL=1 launches in plain stream order.
+template <typename Kern, typename... Args>
+void launch_pdl(Kern kern, dim3 grid, int tpb, size_t smem, void* stream, const Args&... args) {
+    static const bool off = [] {
+        const char* e = std::getenv("TOMO_NO_PDL");
+        return e && *e && *e != '0';
+    }();
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(tpb);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = off ? 0 : 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, args...);
+    if (e != cudaSuccess && std::getenv("TOMO_DEBUG_LAUNCH")) {
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, kern);
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing((cudaStream_t)stream, &cs);
+        std::fprintf(stderr, "tomo: launch (grid %u x %u, %d threads, %zu B shared; max dynamic %d, static %zu, "
+                     "regs %d, max threads %d, capturing %d) failed: %s\n", grid.x, grid.y, tpb, smem,
+                     fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes, fa.numRegs, fa.maxThreadsPerBlock, (int)cs,
+                     cudaGetErrorString(e));
+    }
+}
+

@@ -34,6 +34,8 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -49,6 +51,7 @@ constexpr int HALO = 8;              // halo (steps per forward launch at most)
 constexpr int RX = TW + 2 * HALO;    // region width: 64 columns (32 lanes x 2 cells)
 constexpr int UOFF = HALO - 1;       // correlation slice: owned rows plus one above and below
 constexpr int TMAXF = TILE_MAX_FWD;
+constexpr size_t MAX_NCH = 2048;     // record channels at most (a launch's rows stay in shared memory)
 static_assert(TMAXF <= HALO, "forward steps per launch exceed the halo");
 
 // Tile shapes: WARPS warps of 4 region rows, region RX x 4 WARPS, owned TW x (4 WARPS - 16).
@@ -205,10 +208,12 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
         const int k = a.k0 + threadIdx.x;          // step threadIdx.x + 1 computes slice k + 1
         ssrc[threadIdx.x] = (int)threadIdx.x < a.T && k < g.n_src_steps ? g.src[k] : 0.f;
     }
-    if (a.gmeas) {
+    if (a.gmeas) {   // measured records: set before the passes, written by no kernel
         const float* gm = a.gmeas + ((int64_t)gl * g.nt + a.k0 + 1) * g.nch;
         for (int i = threadIdx.x; i < a.T * g.nch; i += S::TPB) smeas[i] = gm[i];
     }
+    grid_dep_wait();
+    grid_dep_trigger();
     if (threadIdx.x == 0) {
         mbar_expect_tx(&sm.bar, S::REGION_BYTES + a.w.extra_tx);
         tma_load_3d(sm.u1, &tm.hist, gx0, gy0, gl * a.S + a.k0 % a.S, &sm.bar);
@@ -338,6 +343,8 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
     // residual rows of the launch's steps (z(m) injects rr[m]; row j holds m = kz0-T+1+j), loaded
     // while the copies fly
     float* const srr = reinterpret_cast<float*>(smraw + sizeof(AdjSmem<WARPS>));   // [T][nch]
+    grid_dep_wait();
+    grid_dep_trigger();
     {
         const float* rg = a.rr + gl * a.rrstride + (int64_t)(a.kz0 - a.T + 1) * g.nch;
         for (int i = threadIdx.x; i < a.T * g.nch; i += S::TPB) srr[i] = rg[i];
@@ -504,7 +511,8 @@ bool encode(EncodeTiled fn, unsigned char* out, CUtensorMapDataType type, const 
 bool tile_supported(const DevGeo& g, int profile) {
     // nx % 4 == 0: 16-byte row strides and tile origins (multiples of 4 cells) for the TMA copies;
     // nch <= 2048: a launch's record rows (8 x nch floats) fit in shared memory next to the region
-    return profile == TOMO_PROFILE_CFG && g.rid != nullptr && g.dmap != nullptr && g.nx % 4 == 0 && g.nch <= 2048;
+    return profile == TOMO_PROFILE_CFG && g.rid != nullptr && g.dmap != nullptr && g.nx % 4 == 0 &&
+           g.nch <= (int)MAX_NCH;
 }
 
 bool encode_tile_maps(TileMaps* m, const DevGeo& g, const float* hist, int64_t hist_planes, const float* z,
@@ -532,6 +540,13 @@ bool encode_tile_maps(TileMaps* m, const DevGeo& g, const float* hist, int64_t h
 }
 
 namespace {
+// Dynamic shared memory of a launch at most: the region and exchange rows, plus 8 source values
+// and the record rows of up to 8 (forward) or 6 (adjoint) steps of up to MAX_NCH channels.
+template <int WARPS>
+constexpr size_t fwd_smem_cap() { return sizeof(FwdSmem<WARPS>) + 4 * (TMAXF + TMAXF * MAX_NCH); }
+template <int WARPS>
+constexpr size_t adj_smem_cap() { return sizeof(AdjSmem<WARPS>) + 4 * 6 * MAX_NCH; }
+
 template <int WARPS>
 void fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream) {
     using S = Shape<WARPS>;
@@ -539,8 +554,10 @@ void fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream
     TileTma tm;
     std::memcpy(&tm, m.raw[S::SET], sizeof tm);
     const size_t smem = sizeof(FwdSmem<WARPS>) + 4 * (TMAXF + (a.gmeas ? (size_t)a.T * g.nch : 0));
-    cudaFuncSetAttribute(k_fwd_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_fwd_tile<WARPS><<<dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, (cudaStream_t)stream>>>(g, tm, a, tiles_x);
+    // one fixed cap (the largest any launch asks for) rather than this launch's size: contexts on
+    // other host threads launch the same kernel with other sizes
+    cudaFuncSetAttribute(k_fwd_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem_cap<WARPS>());
+    launch_pdl(k_fwd_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
 }
 template <int WARPS>
 void adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream) {
@@ -549,8 +566,8 @@ void adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream
     TileTma tm;
     std::memcpy(&tm, m.raw[S::SET], sizeof tm);
     const size_t smem = sizeof(AdjSmem<WARPS>) + 4 * (size_t)a.T * g.nch;
-    cudaFuncSetAttribute(k_adj_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_adj_tile<WARPS><<<dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, (cudaStream_t)stream>>>(g, tm, a, tiles_x);
+    cudaFuncSetAttribute(k_adj_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_smem_cap<WARPS>());
+    launch_pdl(k_adj_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
 }
 }  // namespace
 
