@@ -44,7 +44,8 @@ DRIVERS = {
     "sirt-mimo-norm-alt": "SIRT_MIMO_NORM_ALT",
     "tomo": "TOMO_MULTI",
 }
-HEADERS = [os.path.join(INCLUDE, "tomo.h"), os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "cell.cuh")]
+HEADERS = [os.path.join(INCLUDE, "tomo.h"), os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "cell.cuh"),
+           os.path.join(CSRC, "async.cuh"), os.path.join(CSRC, "cnn.h")]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

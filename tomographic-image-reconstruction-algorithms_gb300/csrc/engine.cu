@@ -1743,6 +1743,7 @@ tomo_status tomo_iterate_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule
     CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
     TRY(sync_check(c));
     CU(c, cudaGetLastError());
+    if ((ns = net_check(net)) != TOMO_OK) return c->fail(ns, "network: %s", tomo_net_last_error(net));
     if (accepted) *accepted = ok ? 1 : 0;
     if (stats) {
         float ms = 0.f;
@@ -1821,6 +1822,7 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
     CU(c, cudaMemcpyAsync(d_f, c->f, fb, cudaMemcpyDeviceToDevice, c->st));
     TRY(sync_check(c));
     CU(c, cudaGetLastError());
+    if (tomo_status ns = net_check(net); ns != TOMO_OK) return c->fail(ns, "network: %s", tomo_net_last_error(net));
     if (iters_done) *iters_done = done;
     if (sweeps) *sweeps = nsweep;
     if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

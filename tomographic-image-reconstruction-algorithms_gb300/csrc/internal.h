@@ -227,6 +227,9 @@ void launch_features(const float* f, const float* dir, const unsigned int* dmax,
                      int64_t N, float* feat, void* stream);
 // learned update network (net.cu): one image, features planar [3][H][W], output [H][W]
 tomo_status net_infer(tomo_net* net, const float* feat, int H, int W, float* out, void* stream);
+// TOMO_ERR_TIMEOUT when a network kernel's bounded wait ran out since the last check (call after
+// the stream the network ran on has been synchronised), else TOMO_OK.
+tomo_status net_check(tomo_net* net);
 
 // warp-strip step kernels (strip.cu): CFG profile, nx % 4 == 0; rows per warp in {2,4,8,16,32}
 bool strip_supported(const DevGeo& g, int profile);
@@ -301,6 +304,9 @@ bool encode_tile_maps(TileMaps* m, const DevGeo& g, const float* hist, int64_t h
                       int64_t z_planes, const float* coef, std::string* why);
 void launch_fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream);
 void launch_adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream);
+// cuTensorMapEncodeTiled, looked up from the driver once (no link against libcuda); null when
+// the driver has none.
+void* tensor_map_encoder();
 constexpr int TILE_OWNED = 48;    // owned tile width and height of the tile kernels
 constexpr int TILE_MAX_FWD = 8;   // forward steps per tile launch at most
 

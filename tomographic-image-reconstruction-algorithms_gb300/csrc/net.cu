@@ -10,34 +10,17 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
 #include <vector>
 
+#include "cnn.h"
 #include "internal.h"
-
-namespace tomo {
-namespace cnn {
-void pack_input(const float* feat, __nv_bfloat16* x, int B, int H, int W, cudaStream_t st);
-void conv32_relu(int cin, const __nv_bfloat16* in, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* out, int B,
-                 int H, int W, cudaStream_t st);
-void conv32_dgrad(const __nv_bfloat16* dz, const __nv_bfloat16* wd, const __nv_bfloat16* mask, __nv_bfloat16* out, int B,
-                  int H, int W, cudaStream_t st);
-void conv_out(const __nv_bfloat16* y4, const float* w5, const float* b5, float* out, int B, int H, int W, cudaStream_t st);
-void loss(const float* out, const float* tgt, const float* msk, int64_t n, float inv_msum, float* dout, double* part,
-          int nblk, double* total, cudaStream_t st);
-void conv_out_backward(const float* dout, const float* w5, const __nv_bfloat16* y4, __nv_bfloat16* dz4, float* part,
-                       int nblk, float* grad_w5b5, int B, int H, int W, cudaStream_t st);
-void conv32_wgrad(int cin, const __nv_bfloat16* x, const __nv_bfloat16* dz, float* part, int nblk, float* grad_wb, int B,
-                  int H, int W, cudaStream_t st);
-void adam(float* w, float* m, float* v, const float* g, int n, float lr, float b1, float b2, float eps, float c1, float c2,
-          cudaStream_t st);
-void pack_weights(const float* wm, int cin, __nv_bfloat16* wf, __nv_bfloat16* wd, cudaStream_t st);
-}  // namespace cnn
-}  // namespace tomo
 
 using namespace tomo;
 
@@ -59,18 +42,29 @@ struct tomo_net {
     cudaStream_t st = nullptr;
     std::string err;
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;   // FP32 master, grad, Adam moments
-    __nv_bfloat16 *wf1 = nullptr, *wf[3] = {}, *wd[3] = {};          // BF16 forward / data-gradient weights
+    // BF16 tensor-core operands: forward and data-gradient weights of layers 1-4, output layer
+    __nv_bfloat16 *wf1 = nullptr, *wf[3] = {}, *wd[3] = {}, *wo = nullptr, *wod = nullptr;
     float* part = nullptr;                                            // weight-gradient partials
     double *lpart = nullptr, *ltot = nullptr;
-    // activations for the current capacity (pixels)
+    // error word of the kernels' bounded waits (mapped host memory: host and device addresses)
+    unsigned int *errh = nullptr, *errd = nullptr;
+    uint64_t wait_ns = 1000000000ull;                                 // TOMO_WAIT_LIMIT_NS
+    // activations for the current capacity (pixels); dpk = packed loss gradient [P][16]
     int64_t cap = 0;
-    __nv_bfloat16 *x0 = nullptr, *y[4] = {}, *dz[2] = {};
+    __nv_bfloat16 *x0 = nullptr, *y[4] = {}, *dz[2] = {}, *dpk = nullptr;
     float *out = nullptr, *dout = nullptr, *msk_sum = nullptr;
+    // TMA maps of the activations for shape (mB, mH, mW): convolution-input boxes and
+    // weight-gradient boxes
+    enum { M_X0, M_Y0, M_Y1, M_Y2, M_Y3, M_DZ0, M_DZ1, M_DPK, NMAPS };
+    alignas(64) unsigned char cmap[NMAPS][128];
+    alignas(64) unsigned char wmap[NMAPS][128];
+    int mB = 0, mH = 0, mW = 0;
     int64_t step = 0;
     std::vector<void*> allocs;
     ~tomo_net() {
         cudaSetDevice(dev);
         for (void* p : allocs) cudaFree(p);
+        if (errh) cudaFreeHost(errh);
         if (st) cudaStreamDestroy(st);
     }
     template <typename T>
@@ -92,6 +86,12 @@ struct tomo_net {
         for (auto& a : allocs)
             if (a == p) { cudaFree(a); a = nullptr; }
     }
+    // a timed-out wait of a network kernel since the last check (clears the word)
+    bool timed_out() {
+        if (!errh || *(volatile unsigned int*)errh == 0u) return false;
+        *(volatile unsigned int*)errh = 0u;
+        return true;
+    }
 };
 
 namespace {
@@ -111,34 +111,61 @@ void repack(tomo_net* n, cudaStream_t st) {
     cnn::pack_weights(n->w + oW1, 16, n->wf1, nullptr, st);
     const int64_t ow[3] = {oW2, oW3, oW4};
     for (int l = 0; l < 3; ++l) cnn::pack_weights(n->w + ow[l], C, n->wf[l], n->wd[l], st);
+    cnn::pack_out_weights(n->w + oW5, n->wo, n->wod, st);
 }
 
 tomo_status ensure_capacity(tomo_net* n, int64_t pixels) {
     if (pixels <= n->cap) return TOMO_OK;
     for (void* p : {(void*)n->x0, (void*)n->y[0], (void*)n->y[1], (void*)n->y[2], (void*)n->y[3], (void*)n->dz[0],
-                    (void*)n->dz[1], (void*)n->out, (void*)n->dout})
+                    (void*)n->dz[1], (void*)n->dpk, (void*)n->out, (void*)n->dout})
         if (p) n->release(p);
+    n->mB = n->mH = n->mW = 0;   // the maps name the released buffers
     bool ok = n->alloc(&n->x0, pixels * 16);
     for (int l = 0; l < 4; ++l) ok = ok && n->alloc(&n->y[l], pixels * C);
-    ok = ok && n->alloc(&n->dz[0], pixels * C) && n->alloc(&n->dz[1], pixels * C);
+    ok = ok && n->alloc(&n->dz[0], pixels * C) && n->alloc(&n->dz[1], pixels * C) && n->alloc(&n->dpk, pixels * 16);
     ok = ok && n->alloc(&n->out, pixels) && n->alloc(&n->dout, pixels);
     if (!ok) return n->fail(TOMO_ERR_OOM, "network activations do not fit");
     n->cap = pixels;
     return TOMO_OK;
 }
 
+// TMA maps of every activation for images B x H x W (re-encoded when the shape changes).
+tomo_status ensure_maps(tomo_net* n, int B, int H, int W) {
+    if (n->mB == B && n->mH == H && n->mW == W) return TOMO_OK;
+    const __nv_bfloat16* base[tomo_net::NMAPS] = {n->x0, n->y[0], n->y[1], n->y[2], n->y[3], n->dz[0], n->dz[1], n->dpk};
+    const int ch[tomo_net::NMAPS] = {16, C, C, C, C, C, C, 16};
+    for (int i = 0; i < tomo_net::NMAPS; ++i)
+        if (!cnn::encode_act_map(n->cmap[i], base[i], ch[i], B, H, W, true) ||
+            !cnn::encode_act_map(n->wmap[i], base[i], ch[i], B, H, W, false)) {
+            n->mB = n->mH = n->mW = 0;
+            return n->fail(TOMO_ERR_CUDA, "cuTensorMapEncodeTiled refused an activation map");
+        }
+    n->mB = B;
+    n->mH = H;
+    n->mW = W;
+    return TOMO_OK;
+}
+
 tomo_status check_shape(tomo_net* n, int B, int H, int W) {
     if (B < 1 || H < 1 || W < 64 || W % 64 != 0) return n->fail(TOMO_ERR_ARG, "images must be W % 64 == 0 wide");
-    return ensure_capacity(n, (int64_t)B * H * W);
+    if ((int64_t)B * H > (int64_t)1 << 24 || W > 1 << 20) return n->fail(TOMO_ERR_ARG, "images too large");
+    tomo_status s = ensure_capacity(n, (int64_t)B * H * W);
+    return s != TOMO_OK ? s : ensure_maps(n, B, H, W);
+}
+
+tomo_status check_waits(tomo_net* n) {
+    return n->timed_out() ? n->fail(TOMO_ERR_TIMEOUT, "network kernel: a TMA copy or MMA did not complete in time")
+                          : TOMO_OK;
 }
 
 void forward(tomo_net* n, const float* feat, int B, int H, int W, float* out, cudaStream_t st) {
     cnn::pack_input(feat, n->x0, B, H, W, st);
-    cnn::conv32_relu(16, n->x0, n->wf1, n->w + ob1, n->y[0], B, H, W, st);
-    cnn::conv32_relu(C, n->y[0], n->wf[0], n->w + ob2, n->y[1], B, H, W, st);
-    cnn::conv32_relu(C, n->y[1], n->wf[1], n->w + ob3, n->y[2], B, H, W, st);
-    cnn::conv32_relu(C, n->y[2], n->wf[2], n->w + ob4, n->y[3], B, H, W, st);
-    cnn::conv_out(n->y[3], n->w + oW5, n->w + ob5, out, B, H, W, st);
+    const float* bias[4] = {n->w + ob1, n->w + ob2, n->w + ob3, n->w + ob4};
+    cnn::conv(cnn::CONV_IN, n->cmap[tomo_net::M_X0], n->wf1, bias[0], nullptr, n->y[0], B, H, W, n->errd, n->wait_ns, st);
+    for (int l = 0; l < 3; ++l)
+        cnn::conv(cnn::CONV_MID, n->cmap[tomo_net::M_Y0 + l], n->wf[l], bias[l + 1], nullptr, n->y[l + 1], B, H, W,
+                  n->errd, n->wait_ns, st);
+    cnn::conv(cnn::CONV_OUT, n->cmap[tomo_net::M_Y3], n->wo, n->w + ob5, nullptr, out, B, H, W, n->errd, n->wait_ns, st);
 }
 
 // loss and gradient into n->g
@@ -154,21 +181,29 @@ tomo_status backward(tomo_net* n, const float* feat, const float* tgt, const flo
     for (float x : hm) ms += x;
     if (!(ms > 0.0)) return n->fail(TOMO_ERR_ARG, "mask is empty");
     forward(n, feat, B, H, W, n->out, st);
-    cnn::loss(n->out, tgt, msk, P, (float)(1.0 / ms), n->dout, n->lpart, kPartBlocks, n->ltot, st);
-    cnn::conv_out_backward(n->dout, n->w + oW5, n->y[3], n->dz[0], n->part, kPartBlocks, n->g + oW5, B, H, W, st);
+    cnn::loss(n->out, tgt, msk, P, (float)(1.0 / ms), n->dout, n->dpk, n->lpart, kPartBlocks, n->ltot, st);
+    // layer 5: weight gradient from the packed loss gradient, then the data gradient into layer 4
+    cnn::wgrad(cnn::WGRAD_OUT, n->wmap[tomo_net::M_Y3], n->wmap[tomo_net::M_DPK], n->part, kPartBlocks, n->g + oW5, B,
+               H, W, n->errd, n->wait_ns, st);
+    cnn::conv(cnn::CONV_OUT_DGRAD, n->cmap[tomo_net::M_DPK], n->wod, nullptr, n->y[3], n->dz[0], B, H, W, n->errd,
+              n->wait_ns, st);
     // layers 4, 3, 2: weight gradient, then data gradient masked by the layer input's ReLU
     const int64_t ow[3] = {oW2, oW3, oW4};
     int cur = 0;
     for (int l = 2; l >= 0; --l) {   // l = index of layers 2..4 in wf/wd; input activation y[l]
-        cnn::conv32_wgrad(C, n->y[l], n->dz[cur], n->part, kPartBlocks, n->g + ow[l], B, H, W, st);
-        cnn::conv32_dgrad(n->dz[cur], n->wd[l], n->y[l], n->dz[1 - cur], B, H, W, st);
+        cnn::wgrad(cnn::WGRAD_MID, n->wmap[tomo_net::M_Y0 + l], n->wmap[tomo_net::M_DZ0 + cur], n->part, kPartBlocks,
+                   n->g + ow[l], B, H, W, n->errd, n->wait_ns, st);
+        cnn::conv(cnn::CONV_DGRAD, n->cmap[tomo_net::M_DZ0 + cur], n->wd[l], nullptr, n->y[l], n->dz[1 - cur], B, H, W,
+                  n->errd, n->wait_ns, st);
         cur = 1 - cur;
     }
-    cnn::conv32_wgrad(16, n->x0, n->dz[cur], n->part, kPartBlocks, n->g + oW1, B, H, W, st);
+    cnn::wgrad(cnn::WGRAD_IN, n->wmap[tomo_net::M_X0], n->wmap[tomo_net::M_DZ0 + cur], n->part, kPartBlocks, n->g + oW1,
+               B, H, W, n->errd, n->wait_ns, st);
     double l = 0.0;
     NCU(n, cudaMemcpyAsync(&l, n->ltot, sizeof(double), cudaMemcpyDeviceToHost, st));
     NCU(n, cudaStreamSynchronize(st));
     NCU(n, cudaGetLastError());
+    if (tomo_status w = check_waits(n); w != TOMO_OK) return w;
     if (loss_out) *loss_out = l / ms;
     return TOMO_OK;
 }
@@ -183,6 +218,7 @@ tomo_status net_infer(tomo_net* n, const float* feat, int H, int W, float* out, 
     forward(n, feat, 1, H, W, out, (cudaStream_t)stream);
     return TOMO_OK;
 }
+tomo_status net_check(tomo_net* n) { return check_waits(n); }
 }  // namespace tomo
 
 // ---- C ABI -----------------------------------------------------------------------------
@@ -205,9 +241,21 @@ tomo_status tomo_net_create(int32_t device, uint64_t seed, tomo_net** out) try {
     bool ok = n->alloc(&n->w, kParams) && n->alloc(&n->g, kParams) && n->alloc(&n->m, kParams) &&
               n->alloc(&n->v, kParams) && n->alloc(&n->wf1, kW1);
     for (int l = 0; l < 3; ++l) ok = ok && n->alloc(&n->wf[l], kWmid) && n->alloc(&n->wd[l], kWmid);
+    ok = ok && n->alloc(&n->wo, 9 * 16 * C) && n->alloc(&n->wod, 9 * 16 * C);
     ok = ok && n->alloc(&n->part, (int64_t)kPartBlocks * (kWmid + C)) && n->alloc(&n->lpart, kPartBlocks) &&
          n->alloc(&n->ltot, 1);
     if (!ok) return TOMO_ERR_OOM;
+    if (cudaHostAlloc((void**)&n->errh, sizeof(unsigned int), cudaHostAllocMapped) != cudaSuccess) {
+        n->errh = nullptr;
+        cudaGetLastError();
+        return TOMO_ERR_OOM;
+    }
+    *n->errh = 0u;
+    if (cudaHostGetDevicePointer((void**)&n->errd, n->errh, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return TOMO_ERR_CUDA;
+    }
+    if (const char* e = std::getenv("TOMO_WAIT_LIMIT_NS")) n->wait_ns = std::strtoull(e, nullptr, 10);
     // He-normal initialisation for the ReLU layers, small output layer, zero biases
     std::vector<float> h(kParams, 0.f);
     Rng rng(seed);
@@ -272,7 +320,7 @@ tomo_status tomo_net_forward_device(tomo_net* n, const float* d_feat, int32_t B,
     forward(n, d_feat, B, H, W, d_out, n->st);
     NCU(n, cudaStreamSynchronize(n->st));
     NCU(n, cudaGetLastError());
-    return TOMO_OK;
+    return check_waits(n);
 } catch (...) {
     return abi_exception(n ? &n->err : nullptr);
 }
@@ -305,7 +353,7 @@ tomo_status tomo_net_train_step_device(tomo_net* n, const float* d_feat, const f
     repack(n, n->st);
     NCU(n, cudaStreamSynchronize(n->st));
     NCU(n, cudaGetLastError());
-    return TOMO_OK;
+    return check_waits(n);
 } catch (...) {
     return abi_exception(n ? &n->err : nullptr);
 }
