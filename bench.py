@@ -18,7 +18,10 @@ image error, with the speed-up, the gradient sweeps each used and the learned
 run's steps (L learned, x rejected proposal + plain step, p plain step).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl tomo|reference]
-                    [--workload c2|c1|c3|ref192|c5] [--no-cpu] [--no-learned] [--nt T]
+                    [--workload c2|c1|c3|ref192|c5|net] [--no-cpu] [--no-learned] [--nt T]
+--workload net times the learned update network alone (tensor-core kernels): one
+inference on a 512x512 field and one training step on a batch of 16 fields of
+256x256 (shipped weights, synthetic inputs), wall clock per call.
 Under torchrun each rank reconstructs its own independent phantom on its own
 GPU (weak scaling over independent reconstructions, no collective on the
 data path); rank 0 prints one JSON line.
@@ -393,6 +396,52 @@ def art_iteration(ctx, sched, d_f, d_ft, sirt_ms, iters=2):
             "kernel_launches": st.kernel_launches}
 
 
+NET_FLOP_PER_PIXEL = 2 * 9 * (16 * 32 + 3 * 32 * 32 + 32 * 16)   # forward GEMMs as issued (padded channels)
+
+
+def run_net(args):
+    """The learned update network alone: inference on 1 x 512 x 512 and a training step on
+    16 x 256 x 256 (forward, loss, data and weight gradients, Adam), wall clock per call with the
+    call's own synchronisation; FLOP counts are the tensor-core GEMMs as issued (the backward
+    pass issues twice the forward's)."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    net = tomo.Net(0, seed=1)
+    if os.path.exists(WEIGHTS):
+        net.load(WEIGHTS)
+    out = {}
+    for name, (B, H, W) in (("inference_1x512x512", (1, 512, 512)), ("train_16x256x256", (16, 256, 256))):
+        g = torch.Generator(device=dev).manual_seed(7)
+        feat = torch.randn((B, 3, H, W), device=dev, generator=g)
+        res = torch.empty((B, H, W), device=dev)
+        tgt = 0.01 * torch.randn((B, H, W), device=dev, generator=g)
+        msk = torch.ones((B, H, W), device=dev)
+        train = name.startswith("train")
+
+        def call():
+            if train:
+                net.train_step_device(feat.data_ptr(), tgt.data_ptr(), msk.data_ptr(), B, H, W, 1e-6)
+            else:
+                net.forward_device(feat.data_ptr(), B, H, W, res.data_ptr())
+
+        for _ in range(args.warmup):
+            call()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            call()
+        ms = (time.perf_counter() - t0) / args.steps * 1e3
+        flop = (3 if train else 1) * NET_FLOP_PER_PIXEL * B * H * W
+        out[name] = {"ms": ms, "tflops": flop / (ms * 1e-3) / 1e12}
+    net.close()
+    line = {"metric": "learned update network: wall time per call", "value": out["inference_1x512x512"]["ms"],
+            "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+            "dtype": "bf16 (fp32 accumulate)", "data": "synthetic features, shipped weights",
+            "config": {"workload": "net: 5-layer 3x3 CNN, 32 channels, tcgen05 implicit-GEMM kernels"},
+            "calls": out}
+    print(json.dumps(line))
+
+
 def max_over_ranks(x, dist, dev=None):
     """The largest x over all ranks (x itself without a process group)."""
     if not dist:
@@ -429,7 +478,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tomo", choices=["tomo", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "net"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the time-to-image leg (c2)")
     ap.add_argument("--no-art", action="store_true", help="skip the ART iteration leg (c2, c1)")
@@ -467,6 +516,8 @@ def main():
     if not torch.cuda.is_available():
         raise SystemExit("bench.py needs a CUDA GPU (libtomo.so has no CPU path)")
     tomo.lib()
+    if args.workload == "net":
+        return run_net(args)
     if args.workload == "c3":
         run_batch(args, local, rank, world, dist)
         if dist:

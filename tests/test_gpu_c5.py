@@ -1,0 +1,79 @@
+"""GPU checks of the 2048x2048 workload (2048^2 cells, nt 8000, 512 transducers on a
+radius-950 circle in 64 groups of 8, forward history checkpointed every 200 steps).
+
+* The plan the context picks at the workload's full size: the checkpoint interval it was
+  given, how many of the 64 groups each pass keeps resident, and that the plan's buffers fit.
+* Parity at the full grid size with the time axis shortened to 600 steps (the FP64 oracle
+  cannot run 8000 steps of 4 M cells in a test's time): the per-group gradients of the first
+  and the last group at f = f_true / 2 against the oracle, through a plan held to a memory cap
+  so that the 64 groups take several passes (the reference's P-of-M strategy,
+  sirt-mimo-norm-mem.cu:429-458) with checkpoints every 200 steps.
+
+Bars as everywhere else: gradients 1e-4 relative L2; the residual 1e-5.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+import tomo
+
+pytestmark = pytest.mark.gpu
+
+TOL_GRAD = 1e-4
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_lib):
+    return built_lib
+
+
+def c5_config(nt=8000, **kw):
+    return tomo.cfg_config(nx=2048, ny=2048, nt=nt, n_transducers=512, group_size=8, radius=950.0,
+                           ckpt_interval=200, **kw)
+
+
+def c5_phantom():
+    return tomo.phantom_cfg(2048, 2048, 1, 16, 20.0, 240.0, 0.15, 0.01, 760.0, 2001)
+
+
+def test_c5_plan_at_full_size():
+    cfg = c5_config()
+    with tomo.Context(cfg) as ctx:
+        info = ctx.info
+        assert ctx.G == 64 and info.n_transducers == 512
+        assert info.ckpt_interval == 200
+        # every pass keeps P groups' ring of K + 1 slices (16.8 MB each) and their checkpoints
+        P = info.groups_per_pass
+        assert 1 <= P <= 64
+        slice_b = 2048 * 2048 * 4
+        chunks = -(-(8000 - 2) // 200)
+        plan_b = P * (201 + 2 * chunks) * slice_b
+        assert plan_b <= info.device_bytes, (P, plan_b, info.device_bytes)
+        # a GB300 holds most of the groups at once (54 of 64 measured); anything less means the
+        # plan lost memory it should have
+        assert P >= 32, f"only {P} of 64 groups per pass"
+
+
+def test_c5_gradients_full_grid_against_oracle():
+    cfg = c5_config(nt=600, mem_limit_mb=40 * 1024)   # about 11 groups per pass: 6 passes
+    fo = c5_phantom()
+    with tomo.Context(cfg) as ctx:
+        P = ctx.info.groups_per_pass
+        assert ctx.info.ckpt_interval == 200 and 1 <= P < 64, P
+        rec = ctx.forward(fo)
+        f_half = (0.5 * fo).astype(np.float32)
+        dfg, _, r2 = ctx.gradient(f_half, rec)
+    assert np.isfinite(dfg).all()
+    d0, r0 = O.gradient_groups(cfg, f_half.astype(np.float64), rec, 0, 1)
+    d63, r63 = O.gradient_groups(cfg, f_half.astype(np.float64), rec, 63, 1)
+    eps = 100.0 * rel(f_half, fo)
+    for g, want in ((0, d0[0]), (63, d63[0])):
+        e = rel(dfg[g], want)
+        assert e <= TOL_GRAD, (f"gradient of group {g} ({P} groups per pass): {e:.2e}; "
+                               f"image error of f_true / 2 vs phantom {eps:.1f} %")

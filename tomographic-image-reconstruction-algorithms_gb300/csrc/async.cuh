@@ -36,6 +36,9 @@ __device__ __forceinline__ uint64_t gtimer() {
     asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
     return t;
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sm_addr(bar)) : "memory");
+}
 // Waits for phase `parity` of the barrier to complete, at most limit_ns; false on time-out.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
@@ -44,6 +47,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
         if (mbar_try_wait(bar, parity)) return true;
     } while (gtimer() - t0 < limit_ns);
     return false;
+}
+
+// Wait of one role of a warp-specialised kernel: gives up when the barrier has not completed
+// within limit_ns (raising the block's abort flag) or when another role has raised it.
+__device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns, volatile int* abort) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = gtimer();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort) return false;
+        if (gtimer() - t0 >= limit_ns) {
+            *abort = 1;
+            return false;
+        }
+    }
 }
 
 // ---- TMA tile loads (this GPU's own memory; no multicast)
@@ -66,6 +84,14 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
         "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
         "[%6];\n" ::"r"(sm_addr(dst)),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(sm_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];\n" ::"r"(sm_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(sm_addr(bar))
         : "memory");
 }
 // Orders this thread's generic-proxy shared-memory writes before later async-proxy reads (MMA).

@@ -19,9 +19,11 @@ enum ConvKind {
 // Weight gradients on the tensor cores: layer 1 (16 input channels), layers 2-4, layer 5.
 enum WgradKind { WGRAD_IN, WGRAD_MID, WGRAD_OUT };
 
-// TMA map of an NHWC BF16 activation [B][H][W][C] (C % 8 == 0): boxes of 8 channels x 130
-// pixels x 3 rows (convolution input) or 8 channels x 128 pixels (weight-gradient operand);
-// false when the driver has no encoder or refuses the map.
+// Activations are BF16 in a channel-blocked layout [B][H][C / 8][W][8]: each 8-channel chunk of
+// an image row is W x 16 contiguous bytes.
+// TMA map of an activation (C % 8 == 0): boxes of one row, every chunk, 130 pixels (convolution
+// input: one halo pixel each side) or 128 pixels (weight-gradient operand); false when the
+// driver has no encoder or refuses the map.
 bool encode_act_map(unsigned char out[128], const __nv_bfloat16* base, int C, int B, int H, int W, bool conv_box);
 
 void pack_input(const float* feat, __nv_bfloat16* x, int B, int H, int W, cudaStream_t st);
@@ -33,9 +35,9 @@ void conv(ConvKind kind, const void* in_map, const __nv_bfloat16* w, const float
 // through per-block partials in part (at most max_blocks rows) reduced in fixed order.
 void wgrad(WgradKind kind, const void* x_map, const void* d_map, float* part, int max_blocks, float* grad, int B, int H,
            int W, unsigned int* err, uint64_t wait_ns, cudaStream_t st);
-// masked MSE: dout (FP32) and its packed BF16 form dpk [P][16] = (dh, dl, dh, 0 ...); the loss
-// sum in *total
-void loss(const float* out, const float* tgt, const float* msk, int64_t n, float inv_msum, float* dout,
+// masked MSE: dout (FP32) and its packed BF16 form dpk (16 channels, blocked) = (dh, dl, dh, 0 ...);
+// the loss sum in *total
+void loss(const float* out, const float* tgt, const float* msk, int64_t n, int W, float inv_msum, float* dout,
           __nv_bfloat16* dpk, double* part, int nblk, double* total, cudaStream_t st);
 void adam(float* w, float* m, float* v, const float* g, int n, float lr, float b1, float b2, float eps, float c1, float c2,
           cudaStream_t st);

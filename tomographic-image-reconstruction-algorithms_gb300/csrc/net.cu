@@ -181,7 +181,7 @@ tomo_status backward(tomo_net* n, const float* feat, const float* tgt, const flo
     for (float x : hm) ms += x;
     if (!(ms > 0.0)) return n->fail(TOMO_ERR_ARG, "mask is empty");
     forward(n, feat, B, H, W, n->out, st);
-    cnn::loss(n->out, tgt, msk, P, (float)(1.0 / ms), n->dout, n->dpk, n->lpart, kPartBlocks, n->ltot, st);
+    cnn::loss(n->out, tgt, msk, P, W, (float)(1.0 / ms), n->dout, n->dpk, n->lpart, kPartBlocks, n->ltot, st);
     // layer 5: weight gradient from the packed loss gradient, then the data gradient into layer 4
     cnn::wgrad(cnn::WGRAD_OUT, n->wmap[tomo_net::M_Y3], n->wmap[tomo_net::M_DPK], n->part, kPartBlocks, n->g + oW5, B,
                H, W, n->errd, n->wait_ns, st);
