@@ -373,7 +373,7 @@ def time_to_image(ctx, w, sched, d_f, d_ft, torch, dev, plain_iters=30):
     reached = bool(leps[-1] <= eps[-1])
     return {"plain_seconds": t_plain, "plain_iters": plain_iters, "target_epsilon": eps[-1],
             "learned_seconds": t_learned, "learned_iters": len(leps),
-            "learned_steps": "".join({1: "L", 0: "x", -1: "p"}[int(k)] for k in kind),
+            "learned_steps": "".join({1: "L", 2: "l", 0: "x", -1: "p"}[int(k)] for k in kind),
             "learned_epsilon": float(leps[-1]), "reached": reached,
             "acceptance": {"min_decrease": tomo.LEARNED_MIN_DECREASE, "patience": tomo.LEARNED_PATIENCE,
                            "scale": tomo.LEARNED_SCALE},

@@ -305,9 +305,13 @@ tomo_status tomo_iterate_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedu
  * rejected proposal falls back to the plain weighted-SIRT step from the saved
  * field (TOMO_SIRT_NORM with `fallback`); after `patience` consecutive
  * rejections (0: never) the run stops proposing and continues with plain
- * steps only.  Per iteration eps_log gets the image error (NaN without
- * d_f_true) and step_log 1 (learned step), 0 (rejected proposal, plain step)
- * or -1 (plain step, no proposal); both optional, at least max_iters entries.
+ * steps only.  With tomo_set_learned_backtrack(ctx, n), a rejected proposal is
+ * first retried up to n times at half the previous scale (one gradient sweep
+ * each, the same network output) before the plain fallback.  Per iteration
+ * eps_log gets the image error (NaN without d_f_true) and step_log 1 (learned
+ * step), 2 (learned step accepted after backtracking), 0 (rejected proposal,
+ * plain step) or -1 (plain step, no proposal); both optional, at least
+ * max_iters entries.
  * *sweeps counts the gradient sweeps (forward + adjoint of all groups) the run
  * made, *seconds its host wall time after the one-off illumination sweep.  The
  * counterpart of tomo_run for the learned update; the reference has none. */
@@ -319,6 +323,11 @@ tomo_status tomo_run_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedule* 
 /* Scale of the learned proposal: tomo_iterate_learned and tomo_run_learned propose
  * f + scale * mask * net(features) (default 1; 0 < scale <= 4). */
 tomo_status tomo_set_learned_scale(tomo_ctx* ctx, double scale);
+
+/* Retries of a rejected learned proposal in tomo_run_learned, each at half the
+ * previous scale, before the plain fallback (default 0; 0 <= retries <= 4).  No
+ * counterpart in the reference. */
+tomo_status tomo_set_learned_backtrack(tomo_ctx* ctx, int32_t retries);
 
 /* Several independent reconstructions advanced together (the batched
  * many-phantom workload: phantoms of different grid sizes, each its own

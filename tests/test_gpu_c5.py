@@ -3,13 +3,19 @@ radius-950 circle in 64 groups of 8, forward history checkpointed every 200 step
 
 * The plan the context picks at the workload's full size: the checkpoint interval it was
   given, how many of the 64 groups each pass keeps resident, and that the plan's buffers fit.
-* Parity at the full grid size with the time axis shortened to 600 steps (the FP64 oracle
-  cannot run 8000 steps of 4 M cells in a test's time): the per-group gradients of the first
-  and the last group at f = f_true / 2 against the oracle, through a plan held to a memory cap
-  so that the 64 groups take several passes (the reference's P-of-M strategy,
+* Parity at the full grid size with the time axis shortened to 1200 steps (the FP64 oracle
+  cannot run 8000 steps of 4 M cells in a test's time; 1200 steps carry a wave 600 cells, past
+  the 380-cell round trip from the transducer ring at radius 950 to the phantom's edge at 760
+  and back, so the records see the phantom): the per-group gradients of the first and the last
+  group at f = f_true / 2 against the oracle, through a plan held to a memory cap so that the
+  64 groups take several passes (the reference's P-of-M strategy,
   sirt-mimo-norm-mem.cu:429-458) with checkpoints every 200 steps.
 
-Bars as everywhere else: gradients 1e-4 relative L2; the residual 1e-5.
+Bars: at 1200 steps the waves have only grazed the phantom, so the residual is a small
+difference of two nearly equal FP32 record sets and FP32 rounding is amplified in it.  The
+oracle measures that amplification itself: its FP32 mode (the same recurrence, rounded in a
+different order from the GPU's fused multiply-adds) against its FP64 result.  The GPU gradient
+must be within max(1e-4, 3 x that distance) of both, and the distance below 1e-2.
 """
 import numpy as np
 import pytest
@@ -61,7 +67,7 @@ def test_c5_plan_at_full_size():
 
 
 def test_c5_gradients_full_grid_against_oracle():
-    cfg = c5_config(nt=600, mem_limit_mb=40 * 1024)   # about 11 groups per pass: 6 passes
+    cfg = c5_config(nt=1200, mem_limit_mb=40 * 1024)   # about 11 groups per pass: 6 passes
     fo = c5_phantom()
     with tomo.Context(cfg) as ctx:
         P = ctx.info.groups_per_pass
@@ -72,8 +78,17 @@ def test_c5_gradients_full_grid_against_oracle():
     assert np.isfinite(dfg).all()
     d0, r0 = O.gradient_groups(cfg, f_half.astype(np.float64), rec, 0, 1)
     d63, r63 = O.gradient_groups(cfg, f_half.astype(np.float64), rec, 63, 1)
+    d0_32, _ = O.gradient_groups(cfg, f_half.astype(np.float64), rec, 0, 1, prec=32)
+    # the records of f_true / 2 differ from those of f_true: the comparison is not of noise
+    assert r0 > 1e-6 * float(np.sum(np.asarray(rec[0], np.float64) ** 2)), r0
     eps = 100.0 * rel(f_half, fo)
+    cond = rel(d0_32[0], d0[0])                 # the problem's FP32 conditioning
+    bound = max(TOL_GRAD, 3.0 * cond)
+    assert cond <= 1e-2, cond
+    e32 = rel(dfg[0], d0_32[0])
+    assert e32 <= bound, (f"gradient of group 0 against the oracle's FP32 mode: {e32:.2e} "
+                          f"({P} groups per pass); FP32 vs FP64 in the oracle {cond:.2e}")
     for g, want in ((0, d0[0]), (63, d63[0])):
         e = rel(dfg[g], want)
-        assert e <= TOL_GRAD, (f"gradient of group {g} ({P} groups per pass): {e:.2e}; "
-                               f"image error of f_true / 2 vs phantom {eps:.1f} %")
+        assert e <= bound, (f"gradient of group {g} ({P} groups per pass): {e:.2e} against FP64, bound "
+                            f"{bound:.2e}; image error of f_true / 2 vs phantom {eps:.1f} %")

@@ -175,6 +175,45 @@ def test_run_learned_stops_at_target(torch_dev):
                                 1e-2, 10, **bad)
 
 
+def test_run_learned_backtracks_to_a_smaller_proposal(torch_dev):
+    """A rejected proposal is retried at half the scale before the plain fallback: with the
+    network proposing exactly the missing field, scale 4 overshoots and is rejected; the
+    retries land bit for bit on what a run at the accepted scale computes."""
+    torch, dev = torch_dev
+    cfg = cfg_small()
+    m = O.mask(cfg).astype(np.float32)
+    fo = (0.03 * m).astype(np.float32)
+    sched = tomo.schedule(omega=0.02, normalize=1)
+    with tomo.Context(cfg) as ctx:
+        ctx.set_records(ctx.forward(fo))
+        net = tomo.Net(0, seed=1)
+        p = np.zeros(net.n_params, np.float32)
+        p[-1] = 0.03                             # the network proposes exactly the missing field
+        net.set_params(p)
+        d_ft = torch.from_numpy(fo).to(dev)
+
+        def one(scale, back):
+            ctx.set_learned_scale(scale)
+            ctx.set_learned_backtrack(back)
+            d_f = torch.zeros(fo.shape, dtype=torch.float32, device=dev)
+            _, kind, sweeps, _ = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), -1.0, 1)
+            return int(kind[0]), sweeps, d_f.cpu().numpy()
+
+        k1, s1, f1 = one(1.0, 0)
+        k2, s2, f2 = one(2.0, 0)
+        k4, s4, f4 = one(4.0, 0)
+        kb, sb, fb = one(4.0, 2)
+        assert k1 == 1 and s1 == 2 and k4 == 0
+        if k2 == 1:                              # accepted at half of 4
+            assert (kb, sb) == (2, 3) and np.array_equal(fb, f2)
+        else:                                    # accepted at a quarter of 4
+            assert (kb, sb) == (2, 4) and np.array_equal(fb, f1)
+        ctx.set_learned_scale(tomo.LEARNED_SCALE)
+        ctx.set_learned_backtrack(0)
+        with pytest.raises(tomo.TomoError):
+            ctx.set_learned_backtrack(5)
+
+
 def test_shipped_network_gain(torch_dev):
     """What the trained network gains on the 512x512 / 256-transducer workload: the learned
     update reaches the image error of 30 plain weighted-SIRT iterations with at most half the

@@ -86,6 +86,7 @@ struct tomo_ctx {
     unsigned int *illum_max = nullptr, *maxsave = nullptr;
     bool illum_ready = false;
     double learned_scale = 1.0;  // the network's proposal is f + learned_scale * mask * net(features)
+    int learned_backtrack = 0;   // retries of a rejected proposal at half the scale (tomo_run_learned)
     static constexpr int ZR = 4; // adjoint ring slots
     TileMaps tmaps;              // TMA maps of hist, z, coef, dmap, rid (tile kernels)
     unsigned int* err_host = nullptr;   // tile kernels' wait time-out word (mapped pinned memory)
@@ -1791,14 +1792,25 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
             CU(c, cudaMemcpyAsync(c->fsave, c->f, fb, cudaMemcpyDeviceToDevice, c->st));
             CU(c, cudaMemcpyAsync(c->dsave, c->dir, fb, cudaMemcpyDeviceToDevice, c->st));
             CU(c, cudaMemcpyAsync(c->maxsave, c->maxabs, sizeof(unsigned int), cudaMemcpyDeviceToDevice, c->st));
-            launch_apply(c->f, c->dnet, c->mask, N, c->learned_scale, nullptr, c->st);
-            c->launches += 7;
-            // the check is the gradient sweep of the proposal: accepted, it is the next step's gradient
-            TRY(features_core(c, &r1));
-            ++nsweep;
-            kind = r1 <= (1.0 - min_decrease) * r0 ? 1 : 0;
+            c->launches += 6;
+            double sc = c->learned_scale;
+            for (int tries = 0;; ++tries) {
+                if (tries > 0) CU(c, cudaMemcpyAsync(c->f, c->fsave, fb, cudaMemcpyDeviceToDevice, c->st));
+                launch_apply(c->f, c->dnet, c->mask, N, sc, nullptr, c->st);
+                ++c->launches;
+                // the check is the gradient sweep of the proposal: accepted, it is the next step's gradient
+                TRY(features_core(c, &r1));
+                ++nsweep;
+                if (r1 <= (1.0 - min_decrease) * r0) {
+                    kind = tries == 0 ? 1 : 2;
+                    break;
+                }
+                kind = 0;
+                if (tries >= c->learned_backtrack) break;
+                sc *= 0.5;   // the same network output at half the scale
+            }
         }
-        if (kind == 1) {
+        if (kind >= 1) {
             r0 = r1;
             rejected = 0;
         } else {
@@ -1937,6 +1949,13 @@ tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const
     return TOMO_OK;
 } catch (...) {
     return abi_exception(nullptr);
+}
+
+tomo_status tomo_set_learned_backtrack(tomo_ctx* c, int32_t retries) {
+    if (!c) return TOMO_ERR_ARG;
+    if (retries < 0 || retries > 4) return c->fail(TOMO_ERR_ARG, "learned backtrack retries must be in 0..4");
+    c->learned_backtrack = retries;
+    return TOMO_OK;
 }
 
 tomo_status tomo_set_learned_scale(tomo_ctx* c, double scale) {

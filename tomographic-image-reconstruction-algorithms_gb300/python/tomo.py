@@ -183,6 +183,7 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_net_train_step_device": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, DP]),
         "tomo_features_device": (i32, [vp, vp, vp, DP]),
         "tomo_set_learned_scale": (i32, [vp, C.c_double]),
+        "tomo_set_learned_backtrack": (i32, [vp, i32]),
         "tomo_iterate_learned": (i32, [vp, vp, C.POINTER(Schedule), i32, vp, vp, C.POINTER(IterStats), IP]),
         "tomo_run_learned": (i32, [vp, vp, C.POINTER(Schedule), vp, vp, C.c_double, i32, C.c_double, i32, DP, IP,
                                    IP, IP, C.POINTER(C.c_double)]),
@@ -393,6 +394,10 @@ class Context:
     def set_learned_scale(self, scale: float):
         """Scale of the learned proposal f + scale * mask * net(features)."""
         self._check(lib().tomo_set_learned_scale(self.h, scale))
+
+    def set_learned_backtrack(self, retries: int):
+        """Retries of a rejected learned proposal at half the previous scale (run_learned)."""
+        self._check(lib().tomo_set_learned_backtrack(self.h, int(retries)))
 
     @property
     def stream(self) -> int:
