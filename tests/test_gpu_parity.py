@@ -239,6 +239,32 @@ def test_checkpoint_and_passes_match_full_history(maker):
         assert r2 == ref_r2
 
 
+@pytest.mark.parametrize("maker", [small_ref, small_cfg], ids=["ref", "cfg"])
+def test_art_passes_spread_over_the_slot_buffer(maker, monkeypatch):
+    """ART's one-group passes lay their slices over the whole slot buffer (fewer checkpoints,
+    fewer recomputed steps): two ART iterations under a checkpoint plan equal the
+    resident-history run and the plan's own layout bit for bit."""
+    fo = blob_phantom(maker().ny, maker().nx, seed=7)
+    meas = O.forward(maker(), fo.astype(np.float64))
+    sched = tomo.schedule(omega=0.02, normalize=1)   # each group's direction scaled to max 1
+    outs = []
+    for kw, fixed in ((dict(ckpt_interval=10_000), False), (dict(ckpt_interval=7), False),
+                      (dict(ckpt_interval=7), True)):
+        if fixed:
+            monkeypatch.setenv("TOMO_FIXED_PASS_LAYOUT", "1")
+        else:
+            monkeypatch.delenv("TOMO_FIXED_PASS_LAYOUT", raising=False)
+        with tomo.Context(maker(**kw)) as ctx:
+            ctx.set_records(meas)
+            f = np.zeros_like(fo)
+            eps = [ctx.iterate(tomo.ART, sched, it, f, None, fo).epsilon for it in range(2)]
+            assert np.isfinite(f).all() and eps[1] < 100.0, eps
+            outs.append((f, eps))
+    for f, eps in outs[1:]:
+        assert np.array_equal(f, outs[0][0])
+        assert eps == outs[0][1]
+
+
 @pytest.mark.parametrize("maker,nx,ny", [(small_cfg, 70, 62), (small_ref, 63, 57)], ids=["cfg-70x62", "ref-63x57"])
 def test_per_cell_kernels_on_ragged_grids(maker, nx, ny):
     """Grids whose width is not a multiple of 4 take the per-cell kernels (the warp-strip

@@ -928,11 +928,57 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
     return n;
 }
 
+// Slice layout of one gradient pass.  A pass of fewer groups than the plan keeps resident (the
+// one-group passes of ART, the last pass of a P-of-M plan) spreads its groups' slices over the
+// whole slot buffer, L = P S / ng slots per group: it checkpoints less often and recomputes fewer
+// steps (full history when nt slices fit) in the same memory.  With the fewest chunks L slots
+// allow, K is the smallest interval that still leaves the last chunk in the ring after the
+// forward sweep (nchunk K >= nt - 1), so only the other chunks are recomputed.  Checkpoints
+// hold exact slices, so the pass gives the same bits either way.
+struct PassLayout {
+    int S, K, nchunk;
+    bool full;
+};
+PassLayout pass_layout(const tomo_ctx* c, int mode, int ng) {
+    const PassLayout plan{c->S, c->K, c->nchunk, c->full};
+    if (mode != MODE_GRAD || c->full || ng >= c->P || std::getenv("TOMO_FIXED_PASS_LAYOUT")) return plan;
+    const int nt = c->geo.nt;
+    const int64_t L = (int64_t)c->P * c->S / ng;
+    if (L >= nt) return PassLayout{nt, nt - 2, 1, true};
+    int nchunk = (int)((nt - 2 + L - 2) / (L - 1));
+    int K = (nt - 1 + nchunk - 1) / nchunk;
+    if (K + 1 > L) {
+        ++nchunk;
+        K = (nt - 1 + nchunk - 1) / nchunk;
+    }
+    if (K <= c->K) return plan;
+    return PassLayout{K + 1, K, (nt - 2 + K - 1) / K, false};
+}
+
+// Applies a pass layout to the context while a pass is recorded, and restores the plan's.
+struct LayoutScope {
+    tomo_ctx* c;
+    PassLayout keep;
+    LayoutScope(tomo_ctx* ctx, const PassLayout& l) : c(ctx), keep{ctx->S, ctx->K, ctx->nchunk, ctx->full} {
+        c->S = l.S;
+        c->K = l.K;
+        c->nchunk = l.nchunk;
+        c->full = l.full;
+    }
+    ~LayoutScope() {
+        c->S = keep.S;
+        c->K = keep.K;
+        c->nchunk = keep.nchunk;
+        c->full = keep.full;
+    }
+};
+
 tomo_status run_pass(tomo_ctx* c, int mode, int g0, int ng) {
     const auto key = std::make_tuple(mode, g0, ng);
     auto it = c->graphs.find(key);
     if (it == c->graphs.end()) {
         TRY(autotune(c));
+        LayoutScope layout(c, pass_layout(c, mode, ng));
         cudaGraph_t graph = nullptr;
         CU(c, cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
         const int64_t nk = record_pass(c, mode, g0, ng);
