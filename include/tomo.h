@@ -332,8 +332,14 @@ tomo_status tomo_set_learned_backtrack(tomo_ctx* ctx, int32_t retries);
 /* Several independent reconstructions advanced together (the batched
  * many-phantom workload: phantoms of different grid sizes, each its own
  * context and stream).  Context i runs `iters` iterations of `method` from
- * iteration index iter0 on its device field d_f[i] (records set beforehand),
- * one host thread per context, so the contexts' kernels overlap on the GPU.
+ * iteration index iter0 on its device field d_f[i] (records set beforehand).
+ * When every iteration is device work only (a SIRT method, one device, the
+ * same step for all the call's iterations, no noise redrawn per sweep), one
+ * iteration of every context is recorded into one CUDA graph, a branch per
+ * context, kept with ctxs[0] and replayed once per iteration (recorded again
+ * when the contexts, field pointers, method or step change); otherwise each
+ * context runs on a host thread of its own.  Either way the contexts' kernels
+ * overlap on the GPU and give the same bits as one context at a time.
  * d_f_true (optional, per context) fills eps_log[i * iters + it] (optional).
  * *seconds (optional) is the wall time of the whole batch.  Returns the first
  * failing context's status (its tomo_last_error has the reason).  Replaces

@@ -1,10 +1,22 @@
 """GPU checks of tomo_iterate_batch: independent reconstructions of different grid
 sizes advanced together give the same bits as the same contexts run one after
-another (each context's kernels and reductions are deterministic)."""
+another (each context's kernels and reductions are deterministic), and every
+phantom's images match the FP64 oracle's iterations at the parity bar (1e-4
+relative L2), with the image error against the true phantom in the message."""
 import numpy as np
 import pytest
 
+import oracle_lib as O
 import tomo
+
+TOL_IMG = 1e-4
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
 
 pytestmark = pytest.mark.gpu
 
@@ -60,3 +72,38 @@ def test_batch_rejects_duplicates(built_lib):
         with pytest.raises(tomo.TomoError):
             tomo.iterate_batch([ctx, ctx], tomo.SIRT_NORM, tomo.schedule(omega=0.02, normalize=1), 0, 1,
                                [d.data_ptr(), d.data_ptr()])
+
+
+def test_batch_matches_oracle(built_lib):
+    """Three phantoms of 64^2, 96^2 and 128^2 with the oracle's records: two normalised SIRT
+    iterations through the batch against the oracle's, phantom by phantom."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    sched = tomo.schedule(omega=0.02, normalize=1)
+    ctxs, d_fs, d_fts, want = [], [], [], []
+    for i, cfg in enumerate(configs()):
+        fo = tomo.phantom_cfg(cfg.nx, cfg.ny, 1, 4, cfg.nx / 40, cfg.nx / 8, 0.1, 0.0, 0.8 * cfg.radius, 50 + i)
+        meas = O.forward(cfg, fo.astype(np.float64))
+        f_o = np.zeros(fo.shape, np.float64)
+        eps_o = [O.iterate(cfg, tomo.SIRT_NORM, sched, it, f_o, meas, fo.astype(np.float64))[0] for it in range(2)]
+        want.append((fo, f_o, eps_o))
+        ctx = tomo.Context(cfg)
+        ctx.set_records(meas)
+        ctxs.append(ctx)
+        d_fs.append(torch.zeros(fo.shape, dtype=torch.float32, device=dev))
+        d_fts.append(torch.from_numpy(fo).to(dev))
+    torch.cuda.synchronize(dev)
+    eps, _ = tomo.iterate_batch(ctxs, tomo.SIRT_NORM, sched, 0, 2, [t.data_ptr() for t in d_fs],
+                                [t.data_ptr() for t in d_fts])
+    for c in ctxs:
+        c.synchronize()
+    for i, ((fo, f_o, eps_o), d_f) in enumerate(zip(want, d_fs)):
+        f = d_f.cpu().numpy()
+        msg = (f"phantom {i} ({fo.shape[0]}^2): image vs oracle {rel(f, f_o):.2e}; image error vs phantom "
+               f"gpu {eps[i, -1]:.4f} % oracle {eps_o[-1]:.4f} %")
+        assert rel(f, f_o) <= TOL_IMG, msg
+        for e, eo in zip(eps[i], eps_o):
+            assert abs(e - eo) <= 1e-4 * eo, msg
+    for c in ctxs:
+        c.close()

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -149,16 +150,30 @@ struct tomo_ctx {
     int noise_kind = 0;
     uint64_t noise_seed = 0, noise_draws = 0, noise_key_host = 0;
     uint64_t* noise_key = nullptr;
+    // batched iterations (tomo_iterate_batch): a serial number no later context reuses, a
+    // generation that changes whenever captured launches go stale, the join event of the batch
+    // capture, pinned results of an enqueued iteration (residual, image-error sums), and the
+    // batch graph this context leads (with the key it was recorded for)
+    uint64_t serial = 0, gen = 0;
+    cudaEvent_t evj = nullptr;
+    double* pin = nullptr;
+    std::vector<uint64_t> batch_key;
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<int64_t> batch_kernels;
     void drop_graphs() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
         graphs.clear();
         graph_kernels.clear();
+        ++gen;
     }
     ~tomo_ctx() {
         if (dev >= 0) cudaSetDevice(dev);
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        if (batch_exec) cudaGraphExecDestroy(batch_exec);
         for (void* p : allocs) cudaFree(p);
         if (err_host) cudaFreeHost(err_host);
+        if (pin) cudaFreeHost(pin);
+        if (evj) cudaEventDestroy(evj);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (st) cudaStreamDestroy(st);
@@ -1055,6 +1070,7 @@ tomo_status apply_plan(tomo_ctx* c, const Plan& p) {
     c->release(&c->rr);
     set_plan(c, p);
     c->tuned = false;
+    ++c->gen;
     TRY(alloc_plan_buffers(c));
     encode_maps(c);
     return TOMO_OK;
@@ -1219,22 +1235,14 @@ tomo_status update_core(tomo_ctx* c, int method, const tomo_schedule* sch, doubl
         break;
     case TOMO_SIRT_NORM: {
         // mean, per-group deviation norms, inverse-norm weights (sirt-mimo-norm.cu:56-118)
+        // weights on the device: no host round trip inside the iteration
         launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->tmp, c->st);
         launch_group_dev_norm(c->corr, G, N, c->f, sc, c->tmp, c->part, nb, c->st);
         launch_sum_parts(c->part, G, nb, c->sums, c->st);
-        c->launches += 3;
-        std::vector<double> d2(G);
-        CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
-        TRY(sync_check(c));
-        std::vector<double> w(G);
-        double W = 0.0;
-        for (int gg = 0; gg < G; ++gg) { w[gg] = 1.0 / std::sqrt(d2[gg]); W += w[gg]; }
-        for (int gg = 0; gg < G; ++gg) w[gg] /= W;
-        CU(c, cudaMemcpyAsync(c->sums, w.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
+        launch_norm_weights(c->sums, G, c->st);
         launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
-        ++c->launches;
+        c->launches += 5;
         TRY(apply_dir(c, sch, s));
-        TRY(sync_check(c));   // w lives on the host stack
         break;
     }
     case TOMO_SIRT_AVG_WEIGHT: {
@@ -1268,6 +1276,167 @@ void fill_stats(tomo_ctx* c, tomo_iter_stats* stats, double eps, double r2, doub
 }
 
 // One iteration on c->f with c->meas; f_true in c->ftrue when have_true.
+// One iteration of a SIRT method (not ART) on the context's stream with no host
+// synchronisation, to be recorded into a batch graph: the passes are recorded in place rather
+// than launched as their own graphs, the residual norm and the image-error sums land in pinned
+// memory (pin[0], pin[1..2]).  The same launches, in the same order, as iterate_core.
+tomo_status enqueue_iteration(tomo_ctx* c, int method, const tomo_schedule* sch, double s, float* d_f,
+                              const float* d_ft, int64_t* kernels) {
+    const Geometry& g = c->geo;
+    const int64_t N = g.N, l0 = c->launches;
+    CU(c, cudaMemcpyAsync(c->f, d_f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+    if (d_ft) CU(c, cudaMemcpyAsync(c->ftrue, d_ft, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+    launch_coef(g.cfg.profile, c->f, c->coef, c->rcoef, N, g.cfg.courant, c->st);
+    ++c->launches;
+    for (int g0 = 0; g0 < g.G; g0 += c->P) {
+        const int ng = std::min(c->P, g.G - g0);
+        LayoutScope layout(c, pass_layout(c, MODE_GRAD, ng));
+        c->launches += record_pass(c, MODE_GRAD, g0, ng);
+    }
+    launch_sum_parts(c->rpart, 1, g.G * g.nt, c->sums, c->st);
+    ++c->launches;
+    CU(c, cudaMemcpyAsync(c->pin, c->sums, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    TRY(update_core(c, method, sch, s));
+    if (d_ft) {
+        const int nb = reduce_blocks();
+        launch_eps_parts(c->f, c->ftrue, N, c->part, nb, c->st);
+        launch_sum_parts(c->part, 2, nb, c->sums + 2, c->st);
+        c->launches += 2;
+        CU(c, cudaMemcpyAsync(c->pin + 1, c->sums + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    }
+    CU(c, cudaMemcpyAsync(d_f, c->f, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->st));
+    *kernels = c->launches - l0;
+    return TOMO_OK;
+}
+
+// Records one iteration of every context of a batch into one CUDA graph: a capture on the
+// leading context's stream forks into every context's stream (an event each way), so the
+// phantoms' launches are independent branches of one graph, replayed by one launch per
+// iteration.  The graph stays with the leading context, keyed by the contexts (serial numbers
+// and generations), the field pointers, the method and the step.
+tomo_status record_batch_graph(tomo_ctx** ctxs, int n, int method, const tomo_schedule* sched, double s, float** d_f,
+                               const float** d_ft, const std::vector<uint64_t>& key) {
+    tomo_ctx* lead = ctxs[0];
+    if (lead->batch_exec) {
+        cudaGraphExecDestroy(lead->batch_exec);
+        lead->batch_exec = nullptr;
+        lead->batch_key.clear();
+    }
+    for (int i = 0; i < n; ++i) {
+        tomo_ctx* c = ctxs[i];
+        if (!c->evj) CU(c, cudaEventCreateWithFlags(&c->evj, cudaEventDisableTiming));
+        if (!c->pin) CU(c, cudaHostAlloc((void**)&c->pin, 4 * sizeof(double), cudaHostAllocDefault));
+    }
+    cudaEvent_t fork = nullptr;
+    CU(lead, cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    std::vector<int64_t> kernels(n, 0);
+    tomo_status st = TOMO_OK;
+    cudaGraph_t graph = nullptr;
+    // the capture runs on a stream of its own so that every context (the leading one included)
+    // joins it the same way
+    cudaStream_t cs = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaEventRecord(fork, cs);
+        for (int i = 0; i < n && st == TOMO_OK; ++i) {
+            tomo_ctx* c = ctxs[i];
+            cudaStreamWaitEvent(c->st, fork, 0);
+            st = enqueue_iteration(c, method, sched, s, d_f[i], d_ft ? d_ft[i] : nullptr, &kernels[i]);
+            cudaEventRecord(c->evj, c->st);
+            cudaStreamWaitEvent(cs, c->evj, 0);
+        }
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (st == TOMO_OK && e2 != cudaSuccess) st = lead->cuda(e2, "cudaStreamEndCapture (batch)");
+    } else {
+        st = lead->cuda(e, "batch capture");
+    }
+    if (st == TOMO_OK) {
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e != cudaSuccess) st = lead->cuda(e, "cudaGraphInstantiate (batch)");
+        else {
+            lead->batch_exec = exec;
+            lead->batch_key = key;
+            lead->batch_kernels = kernels;
+        }
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (cs) cudaStreamDestroy(cs);
+    cudaEventDestroy(fork);
+    cudaGetLastError();
+    return st;
+}
+
+// A batch runs as one graph when every iteration is device work only: a SIRT method (not ART),
+// one device, one step size for all the call's iterations (it is recorded in the graph), no
+// noise redrawn per sweep, measured records set.  TOMO_BATCH_THREADS=1 keeps the threaded path.
+bool batch_graph_eligible(tomo_ctx** ctxs, int n, int method, const tomo_schedule* sched, int iter0, int iters) {
+    if (method < TOMO_SIRT_CLASSIC || method > TOMO_SIRT_AVG_WEIGHT || iters < 1) return false;
+    if (const char* e = std::getenv("TOMO_BATCH_THREADS"))
+        if (*e && *e != '0') return false;
+    const double s0 = sched_scale(sched, iter0);
+    if (!std::isfinite(s0)) return false;
+    for (int it = 1; it < iters; ++it)
+        if (sched_scale(sched, iter0 + it) != s0) return false;
+    for (int i = 0; i < n; ++i)
+        if (ctxs[i]->dev != ctxs[0]->dev || ctxs[i]->noise_kind == 2 || !ctxs[i]->meas_set) return false;
+    return true;
+}
+
+// Batch iterations as replays of one recorded graph (record_batch_graph), one launch and one
+// host synchronisation per iteration for all the contexts together.
+tomo_status iterate_batch_graph(tomo_ctx** ctxs, int n, int method, const tomo_schedule* sched, int iter0,
+                                int iters, float** d_f, const float** d_ft, double* eps_log, double* seconds) {
+    tomo_ctx* lead = ctxs[0];
+    const auto t0 = std::chrono::steady_clock::now();
+    CU(lead, cudaSetDevice(lead->dev));
+    const double s = sched_scale(sched, iter0);
+    // kernel choices first: the autotuner times trial passes, which a recording cannot hold
+    for (int i = 0; i < n; ++i) {
+        tomo_ctx* c = ctxs[i];
+        if (!c->tuned) {
+            launch_coef(c->geo.cfg.profile, c->f, c->coef, c->rcoef, c->geo.N, c->geo.cfg.courant, c->st);
+            TRY(autotune(c));
+        }
+    }
+    uint64_t sbits = 0;
+    std::memcpy(&sbits, &s, sizeof sbits);
+    std::vector<uint64_t> key = {(uint64_t)method, sbits, (uint64_t)sched->normalize, (uint64_t)n};
+    for (int i = 0; i < n; ++i) {
+        key.push_back(ctxs[i]->serial);
+        key.push_back(ctxs[i]->gen);
+        key.push_back((uint64_t)(uintptr_t)d_f[i]);
+        key.push_back((uint64_t)(uintptr_t)(d_ft ? d_ft[i] : nullptr));
+    }
+    if (!lead->batch_exec || lead->batch_key != key)
+        TRY(record_batch_graph(ctxs, n, method, sched, s, d_f, d_ft, key));
+    // the graph starts after whatever each context's stream holds
+    for (int i = 0; i < n; ++i) {
+        CU(ctxs[i], cudaEventRecord(ctxs[i]->evj, ctxs[i]->st));
+        CU(lead, cudaStreamWaitEvent(lead->st, ctxs[i]->evj, 0));
+    }
+    for (int it = 0; it < iters; ++it) {
+        CU(lead, cudaGraphLaunch(lead->batch_exec, lead->st));
+        CU(lead, cudaStreamSynchronize(lead->st));
+        for (int i = 0; i < n; ++i) {
+            tomo_ctx* c = ctxs[i];
+            if (c->err_host && *(volatile unsigned int*)c->err_host) {
+                *(volatile unsigned int*)c->err_host = 0u;
+                return c->fail(TOMO_ERR_TIMEOUT, "tile kernel: a TMA copy did not arrive within %llu ns",
+                               (unsigned long long)c->wait_ns);
+            }
+            c->launches += lead->batch_kernels[i];
+            if (eps_log)
+                eps_log[(int64_t)i * iters + it] = d_ft ? 100.0 * std::sqrt(c->pin[1]) / std::sqrt(c->pin[2])
+                                                        : std::numeric_limits<double>::quiet_NaN();
+        }
+    }
+    CU(lead, cudaGetLastError());
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return TOMO_OK;
+}
+
 tomo_status iterate_core(tomo_ctx* c, int method, const tomo_schedule* sch, int it, bool have_true,
                          tomo_iter_stats* stats) {
     const Geometry& g = c->geo;
@@ -1319,16 +1488,9 @@ tomo_status norm_direction(tomo_ctx* c) {
     launch_combine(c->corr, G, N, c->f, sc, nullptr, 1.0 / G, c->tmp, c->st);
     launch_group_dev_norm(c->corr, G, N, c->f, sc, c->tmp, c->part, nb, c->st);
     launch_sum_parts(c->part, G, nb, c->sums, c->st);
-    std::vector<double> d2(G), w(G);
-    CU(c, cudaMemcpyAsync(d2.data(), c->sums, sizeof(double) * G, cudaMemcpyDeviceToHost, c->st));
-    TRY(sync_check(c));
-    double W = 0.0;
-    for (int gg = 0; gg < G; ++gg) { w[gg] = 1.0 / std::sqrt(d2[gg]); W += w[gg]; }
-    for (int gg = 0; gg < G; ++gg) w[gg] /= W;
-    CU(c, cudaMemcpyAsync(c->sums, w.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
+    launch_norm_weights(c->sums, G, c->st);
     launch_combine(c->corr, G, N, c->f, sc, c->sums, 1.0, c->dir, c->st);
-    TRY(sync_check(c));
-    c->launches += 4;
+    c->launches += 5;
     return TOMO_OK;
 }
 
@@ -1443,6 +1605,8 @@ tomo_status tomo_create(const tomo_config* cfg, tomo_ctx** out) try {
         g_create_error = c->err;
         return s;
     }
+    static std::atomic<uint64_t> serials{0};
+    c->serial = ++serials;
     *out = c.release();
     return TOMO_OK;
 } catch (...) {
@@ -1966,6 +2130,8 @@ tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const
         for (int j = 0; j < i; ++j)
             if (ctxs[j] == ctxs[i]) return ctxs[i]->fail(TOMO_ERR_ARG, "a context appears twice in the batch");
     }
+    if (batch_graph_eligible(ctxs, n, method, sched, iter0, iters))
+        return iterate_batch_graph(ctxs, n, method, sched, iter0, iters, d_f, d_f_true, eps_log, seconds);
     std::vector<tomo_status> st(n, TOMO_OK);
     auto work = [&](int i) noexcept {   // the entry points it calls catch their own exceptions
         const float* ft = d_f_true ? d_f_true[i] : nullptr;

@@ -216,6 +216,8 @@ void launch_avgw_apply(const float* corr, int G, int64_t N, float* f, const uint
 void fill_damp(DevGeo& g);
 
 void launch_sum_parts(const double* part, int rows, int nb, double* out, void* stream);
+// squared deviation norms d2[0..G) -> normalised inverse-norm weights, in place (FP64)
+void launch_norm_weights(double* d2w, int G, void* stream);
 void launch_maxabs(const float* dir, const uint8_t* mask, int64_t N, unsigned int* out, void* stream);
 void launch_apply(float* f, const float* dir, const uint8_t* mask, int64_t N, double s,
                   const unsigned int* maxabs, void* stream);

@@ -372,6 +372,19 @@ __global__ void __launch_bounds__(SUM_THREADS) k_sum_parts(const double* __restr
     if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
 }
 
+// Normalised-SIRT group weights in place (sirt-mimo-norm.cu:56-118): d2[g] (squared deviation
+// norms) -> w[g] = (1 / sqrt(d2[g])) / sum_h 1 / sqrt(d2[h]), FP64, the sum in group order.
+__global__ void k_norm_weights(double* __restrict__ d2w, int G) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double W = 0.0;
+    for (int g = 0; g < G; ++g) {
+        const double w = 1.0 / sqrt(d2w[g]);
+        d2w[g] = w;
+        W += w;
+    }
+    for (int g = 0; g < G; ++g) d2w[g] /= W;
+}
+
 __global__ void k_maxabs(const float* __restrict__ dir, const uint8_t* __restrict__ mask, int64_t N,
                          unsigned int* out) {
     float m = 0.f;
@@ -510,6 +523,8 @@ void launch_avgw_apply(const float* corr, int G, int64_t N, float* f, const uint
 void launch_sum_parts(const double* part, int rows, int nb, double* out, void* st) {
     if (rows > 0) k_sum_parts<<<rows, SUM_THREADS, 0, S(st)>>>(part, nb, out);
 }
+
+void launch_norm_weights(double* d2w, int G, void* st) { k_norm_weights<<<1, 32, 0, S(st)>>>(d2w, G); }
 
 void launch_maxabs(const float* dir, const uint8_t* mask, int64_t N, unsigned int* out, void* st) {
     cudaMemsetAsync(out, 0, sizeof(unsigned int), S(st));
