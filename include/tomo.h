@@ -305,7 +305,8 @@ tomo_status tomo_iterate_learned(tomo_ctx* ctx, tomo_net* net, const tomo_schedu
  * rejected proposal falls back to the plain weighted-SIRT step from the saved
  * field (TOMO_SIRT_NORM with `fallback`); after `patience` consecutive
  * rejections (0: never) the run stops proposing and continues with plain
- * steps only.  With tomo_set_learned_backtrack(ctx, n), a rejected proposal is
+ * steps only (or, with tomo_set_learned_resume, proposes again after that
+ * many plain steps).  With tomo_set_learned_backtrack(ctx, n), a rejected proposal is
  * first retried up to n times at half the previous scale (one gradient sweep
  * each, the same network output) before the plain fallback.  Per iteration
  * eps_log gets the image error (NaN without d_f_true) and step_log 1 (learned
@@ -328,6 +329,11 @@ tomo_status tomo_set_learned_scale(tomo_ctx* ctx, double scale);
  * previous scale, before the plain fallback (default 0; 0 <= retries <= 4).  No
  * counterpart in the reference. */
 tomo_status tomo_set_learned_backtrack(tomo_ctx* ctx, int32_t retries);
+
+/* Plain steps after which tomo_run_learned resumes proposing once `patience`
+ * rejections in a row have paused it (default 0: never resume; 0..1000).  No
+ * counterpart in the reference. */
+tomo_status tomo_set_learned_resume(tomo_ctx* ctx, int32_t plain_steps);
 
 /* Several independent reconstructions advanced together (the batched
  * many-phantom workload: phantoms of different grid sizes, each its own

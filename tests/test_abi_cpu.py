@@ -92,6 +92,7 @@ def test_null_handles_are_statuses(built_lib):
         "tomo_synchronize": (None,),
         "tomo_set_learned_scale": (None, 1.0),
         "tomo_set_learned_backtrack": (None, 1),
+        "tomo_set_learned_resume": (None, 3),
         "tomo_gradient_groups_device": (None, None, 0, 1, None),
         "tomo_get_correlations_device": (None, 0, 1, None),
         "tomo_set_correlations_device": (None, 0, 1, None),

@@ -151,6 +151,14 @@ def test_run_learned_rejecting_network_is_plain_sirt(torch_dev):
         assert list(kind) == [0, 0, -1, -1] and sweeps == 1 + 2 * 2 + 2 and secs > 0
         assert np.array_equal(d_f.cpu().numpy(), f_plain)
         assert list(eps) == eps_plain
+        # resuming after one plain step: proposals again (rejected again), still plain SIRT bit for bit
+        ctx.set_learned_resume(1)
+        d_f.zero_()
+        eps, kind, sweeps, _ = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), -1.0, 4)
+        assert list(kind) == [0, 0, -1, 0] and sweeps == 1 + 2 * 2 + 1 + 2
+        assert np.array_equal(d_f.cpu().numpy(), f_plain)
+        assert list(eps) == eps_plain
+        ctx.set_learned_resume(0)
 
 
 def test_run_learned_stops_at_target(torch_dev):

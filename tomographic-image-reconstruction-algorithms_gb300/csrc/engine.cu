@@ -88,6 +88,7 @@ struct tomo_ctx {
     bool illum_ready = false;
     double learned_scale = 1.0;  // the network's proposal is f + learned_scale * mask * net(features)
     int learned_backtrack = 0;   // retries of a rejected proposal at half the scale (tomo_run_learned)
+    int learned_resume = 0;      // plain steps after which paused proposals resume (0: never)
     static constexpr int ZR = 4; // adjoint ring slots
     TileMaps tmaps;              // TMA maps of hist, z, coef, dmap, rid (tile kernels)
     unsigned int* err_host = nullptr;   // tile kernels' wait time-out word (mapped pinned memory)
@@ -1992,6 +1993,7 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
     TRY(features_core(c, &r0));            // gradient, direction and features at the start field
     int done = 0, nsweep = 1, rejected = 0;
     bool learning = true;
+    int paused = 0;                        // plain steps since the proposals paused
     for (int it = 0; it < max_iters; ++it) {
         const double s = sched_scale(fallback, it);
         if (!std::isfinite(s)) return c->fail(TOMO_ERR_ARG, "bad schedule");
@@ -2032,7 +2034,13 @@ tomo_status tomo_run_learned(tomo_ctx* c, tomo_net* net, const tomo_schedule* fa
             ++c->launches;
             TRY(features_core(c, &r0));
             ++nsweep;
-            if (kind == 0 && patience > 0 && ++rejected >= patience) learning = false;   // plain from here on
+            if (kind == 0 && patience > 0 && ++rejected >= patience) {
+                learning = false;   // plain from here on, or for learned_resume plain steps
+                paused = 0;
+            } else if (kind == -1 && c->learned_resume > 0 && ++paused >= c->learned_resume) {
+                learning = true;
+                rejected = 0;
+            }
         }
         double eps = std::numeric_limits<double>::quiet_NaN();
         if (d_f_true) TRY(epsilon(c, &eps));
@@ -2161,6 +2169,13 @@ tomo_status tomo_iterate_batch(tomo_ctx** ctxs, int32_t n, int32_t method, const
     return TOMO_OK;
 } catch (...) {
     return abi_exception(nullptr);
+}
+
+tomo_status tomo_set_learned_resume(tomo_ctx* c, int32_t plain_steps) {
+    if (!c) return TOMO_ERR_ARG;
+    if (plain_steps < 0 || plain_steps > 1000) return c->fail(TOMO_ERR_ARG, "learned resume must be in 0..1000");
+    c->learned_resume = plain_steps;
+    return TOMO_OK;
 }
 
 tomo_status tomo_set_learned_backtrack(tomo_ctx* c, int32_t retries) {

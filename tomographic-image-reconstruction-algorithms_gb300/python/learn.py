@@ -248,8 +248,10 @@ def time_to_image(net, plain_iters=30, seed=2001, device=0,
             md, pat = rule[0], rule[1]
             scale = rule[2] if len(rule) > 2 else LEARNED_SCALE
             back = rule[3] if len(rule) > 3 else 0
+            resume = rule[4] if len(rule) > 4 else 0
             ctx.set_learned_scale(scale)
             ctx.set_learned_backtrack(back)
+            ctx.set_learned_resume(resume)
             d_f.zero_()
             torch.cuda.synchronize(dev)
             leps, kind, sweeps, t_learned = ctx.run_learned(net, sched, d_f.data_ptr(), d_fo.data_ptr(), target,
@@ -257,11 +259,12 @@ def time_to_image(net, plain_iters=30, seed=2001, device=0,
             leps = [float(e) for e in leps]
             reached = bool(leps[-1] <= target)
             steps = "".join({1: "L", 2: "l", 0: "x", -1: "p"}[int(k)] for k in kind)
-            log(f"  learned (min decrease {md}, patience {pat}, scale {scale}, backtrack {back}): {steps}, "
+            log(f"  learned (min decrease {md}, patience {pat}, scale {scale}, backtrack {back}, resume {resume}): "
+                f"{steps}, "
                 f"{sweeps} sweeps, "
                 f"eps -> {leps[-1]:.3f} %, {t_learned:.3f} s, speedup "
                 f"{t_plain / t_learned if reached else float('nan'):.2f}")
-            out["learned"]["%g/%d/%g/%d" % (md, pat, scale, back)] = {
+            out["learned"]["%g/%d/%g/%d/%d" % (md, pat, scale, back, resume)] = {
                 "iters": len(leps), "steps": steps, "sweeps": sweeps, "seconds": t_learned,
                 "final_epsilon": leps[-1], "epsilon": leps, "reached": reached,
                 "speedup": t_plain / t_learned if reached else None}
@@ -284,8 +287,9 @@ def main():
     ap.add_argument("--eval-seeds", default="2001", help="comma-separated phantom seeds of the evaluation")
     ap.add_argument("--eval-scales", default="", help="comma-separated learned-step scales to evaluate "
                                                          "(default: the shipped one)")
-    ap.add_argument("--eval-rules", default="", help="comma-separated scale:backtrack pairs to evaluate "
-                                                        "(backtrack: retries of a rejected proposal at half scale)")
+    ap.add_argument("--eval-rules", default="", help="comma-separated scale:backtrack[:resume] rules to evaluate "
+                                                        "(backtrack: retries of a rejected proposal at half scale; "
+                                                        "resume: plain steps before paused proposals resume)")
     args = ap.parse_args()
     import torch
 
@@ -334,7 +338,8 @@ def main():
         print(f"  evaluation phantom seed {seed}")
         if args.eval_rules:
             rules = tuple((tomo.LEARNED_MIN_DECREASE, tomo.LEARNED_PATIENCE, float(x.split(":")[0]),
-                           int(x.split(":")[1])) for x in args.eval_rules.split(","))
+                           int(x.split(":")[1]), int(x.split(":")[2]) if x.count(":") > 1 else 0)
+                          for x in args.eval_rules.split(","))
         else:
             rules = tuple((tomo.LEARNED_MIN_DECREASE, tomo.LEARNED_PATIENCE, float(x))
                           for x in (args.eval_scales.split(",") if args.eval_scales else [LEARNED_SCALE]))

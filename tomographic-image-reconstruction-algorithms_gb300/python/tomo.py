@@ -184,6 +184,7 @@ def lib(path: str | None = None) -> C.CDLL:
         "tomo_features_device": (i32, [vp, vp, vp, DP]),
         "tomo_set_learned_scale": (i32, [vp, C.c_double]),
         "tomo_set_learned_backtrack": (i32, [vp, i32]),
+        "tomo_set_learned_resume": (i32, [vp, i32]),
         "tomo_iterate_learned": (i32, [vp, vp, C.POINTER(Schedule), i32, vp, vp, C.POINTER(IterStats), IP]),
         "tomo_run_learned": (i32, [vp, vp, C.POINTER(Schedule), vp, vp, C.c_double, i32, C.c_double, i32, DP, IP,
                                    IP, IP, C.POINTER(C.c_double)]),
@@ -398,6 +399,10 @@ class Context:
     def set_learned_backtrack(self, retries: int):
         """Retries of a rejected learned proposal at half the previous scale (run_learned)."""
         self._check(lib().tomo_set_learned_backtrack(self.h, int(retries)))
+
+    def set_learned_resume(self, plain_steps: int):
+        """Plain steps after which a paused learned run proposes again (0: never)."""
+        self._check(lib().tomo_set_learned_resume(self.h, int(plain_steps)))
 
     @property
     def stream(self) -> int:
