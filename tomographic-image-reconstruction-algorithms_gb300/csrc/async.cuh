@@ -64,6 +64,18 @@ __device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, uint64
     }
 }
 
+// Device-scope acquire load (a spin on a counter other blocks release into).
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// Orders this thread's view of global memory (acquired from other blocks) before its later
+// async-proxy reads (TMA copies).
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;\n" ::: "memory");
+}
+
 // ---- TMA tile loads (this GPU's own memory; no multicast)
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
     asm volatile(

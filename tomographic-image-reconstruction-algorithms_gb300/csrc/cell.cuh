@@ -188,3 +188,24 @@ void launch_pdl(Kern kern, dim3 grid, int tpb, size_t smem, void* stream, const 
     }
 }
 
+
+// Cooperative launch: every block is resident at once (the kernel's blocks wait on one another
+// at grid barriers), in stream order after the previous kernel.
+template <typename Kern, typename... Args>
+void launch_coop(Kern kern, dim3 grid, int tpb, size_t smem, void* stream, const Args&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(tpb);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, args...);
+    if (e != cudaSuccess && std::getenv("TOMO_DEBUG_LAUNCH"))
+        std::fprintf(stderr, "tomo: cooperative launch (grid %u x %u, %d threads, %zu B shared) failed: %s\n", grid.x,
+                     grid.y, tpb, smem, cudaGetErrorString(e));
+}
+

@@ -65,16 +65,16 @@ enum { EPI_RELU = 0, EPI_MASK = 1, EPI_OUT = 2 };
 struct ConvArgs {
     const __nv_bfloat16* w;      // B operand, [tap][chunk][N][8] BF16 (K-major core matrices)
     const float* bias;           // EPI_RELU: [N]; EPI_OUT: [1]
-    const __nv_bfloat16* mask;   // EPI_MASK: [B][H][W][N] (output zero where mask <= 0)
-    void* out;                   // EPI_RELU / EPI_MASK: BF16 [B][H][W][N]; EPI_OUT: FP32 [B][H][W]
+    const __nv_bfloat16* mask;   // EPI_MASK: blocked [B][H][N / 8][W][8] (output zero where mask <= 0)
+    void* out;                   // EPI_RELU / EPI_MASK: blocked BF16 [B][H][N / 8][W][8]; EPI_OUT: FP32 [B][H][W]
     int B, H, W;
     unsigned int* err;
     uint64_t wait_ns;
 };
 
 // Row-streaming convolution.  A work item is a strip of up to RC output rows of one 128-pixel
-// column tile of one image; its RC + 2 input rows arrive one TMA box per 8-channel chunk
-// (130 pixels: one halo pixel each side) into a ring of R row slots, each loaded once.
+// column tile of one image; each of its RC + 2 input rows arrives as one TMA box (every
+// 8-channel chunk, 130 pixels: one halo pixel each side) into a ring of R row slots.
 template <int CIN, int N>
 struct ConvShape {
     static constexpr int NCH = CIN / 8;                        // input chunks

@@ -257,11 +257,16 @@ void launch_resid_parts(const float* rr, int ng, int nt, int nch, double* part, 
 // Bounded waits of the tile kernels' TMA copies: a block that waits longer than wait_ns for a
 // copy sets bit 0 of *err (host-visible) and leaves the launch.  extra_tx (0 in production)
 // makes the region copy's barrier expect bytes that never arrive, so a test can run the wait
-// out and check the status.
+// out and check the status.  A persistent launch (k_last / kz_last set) runs a whole segment of
+// chunks with a grid barrier between chunks on the counter *gbar (zeroed before the launch),
+// bounded by the same wait_ns; gbar_extra (0 in production) makes it wait for arrivals that
+// never come.
 struct TileWait {
     unsigned int* err;
     uint64_t wait_ns;
     uint32_t extra_tx;
+    unsigned int* gbar;
+    uint32_t gbar_extra;
 };
 struct TileFwd {
     float* hist;         // forward slots of pass-group 0; slice m at slot m % S
@@ -275,6 +280,7 @@ struct TileFwd {
     const float* gmeas;  // measured records of pass-group 0 (null: simulate)
     float* gout;         // records / residual of pass-group 0 (slices >= 2)
     int warps;           // tile shape: 16 (48 x 48 owned cells) or 10 (48 x 24)
+    int k_last;          // persistent launch: slices k0+1 .. k_last in chunks of T <= 8 (0: one chunk of T)
     TileWait w;
 };
 struct TileAdj {
@@ -290,6 +296,7 @@ struct TileAdj {
     int kz0, T;
     int ng;
     int warps;           // tile shape: 16 (48 x 48 owned cells) or 10 (48 x 24)
+    int kz_last;         // persistent launch: z(kz0) .. z(kz_last) in chunks of 6, 2, 1 (0: one chunk of T)
     TileWait w;
 };
 // TMA tensor maps of one context's buffers (forward slots, adjoint ring, coefficient, sponge
@@ -306,6 +313,8 @@ bool encode_tile_maps(TileMaps* m, const DevGeo& g, const float* hist, int64_t h
                       int64_t z_planes, const float* coef, std::string* why);
 void launch_fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream);
 void launch_adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream);
+// Whether a persistent (cooperative) launch of ng groups keeps every block resident at once.
+bool tile_persistent_fits(const DevGeo& g, int warps, bool fwd, int ng);
 // cuTensorMapEncodeTiled, looked up from the driver once (no link against libcuda); null when
 // the driver has none.
 void* tensor_map_encoder();

@@ -132,12 +132,37 @@ __device__ __forceinline__ void cell_masks(const DevGeo& g, const int* rid, int 
     }
 }
 
+// Grid barrier between the chunks of a persistent launch: every block has issued its chunk's
+// global writes before any block copies its next region (the halo is other blocks' cells).
+// Bounded by wait_ns; false (bit 0 of the error word set) when the arrivals did not all come.
+__device__ __forceinline__ bool grid_sync(const TileWait& w, unsigned int chunk) {
+    __syncthreads();
+    bool ok = true;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(w.gbar, 1u);
+        const unsigned int target = gridDim.x * gridDim.y * chunk + w.gbar_extra;
+        if (ld_acquire(w.gbar) < target) {
+            const uint64_t t0 = gtimer();
+            while (ld_acquire(w.gbar) < target)
+                if (gtimer() - t0 >= w.wait_ns) {
+                    ok = false;
+                    atomicOr(w.err, 1u);
+                    break;
+                }
+        }
+        fence_proxy_async_global();   // this thread's next TMA copies see the other blocks' writes
+    }
+    return __syncthreads_and(ok);
+}
+
+// One forward chunk of a block: slices k0+1 .. k0+T of its tile (the body of a launch); the
+// region barrier completes its phase `parity`.  False when a copy wait timed out.
 template <int WARPS>
-__global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
-    k_fwd_tile(DevGeo g, const __grid_constant__ TileTma tm, TileFwd a, int tiles_x) {
+__device__ __forceinline__ bool fwd_chunk(const DevGeo& g, const TileTma& tm, const TileFwd& a, int tiles_x,
+                                          unsigned char* smraw, uint32_t parity) {
     using S = Shape<WARPS>;
     constexpr int RH = S::RH, TH = S::TH;
-    extern __shared__ __align__(1024) unsigned char smraw[];
     FwdSmem<WARPS>& sm = *reinterpret_cast<FwdSmem<WARPS>*>(smraw);
     const int gl = blockIdx.y;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
@@ -145,11 +170,6 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
     const int64_t N = (int64_t)g.nx * g.ny;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int ggl = a.g0 + gl;
-    if (threadIdx.x == 0) {
-        mbar_init(&sm.bar, 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
     // source amplitudes and measured record rows of the launch's steps, loaded while the copies fly
     // (no global load stays on a step's critical path)
     float* const ssrc = reinterpret_cast<float*>(smraw + sizeof(FwdSmem<WARPS>));   // [TMAXF]
@@ -172,10 +192,10 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
         tma_load_2d(sm.d, &tm.dmap, gx0, gy0, &sm.bar);
         tma_load_2d(sm.rid, &tm.rid, gx0, gy0, &sm.bar);
     }
-    if (!__syncthreads_and(mbar_wait(&sm.bar, 0, a.w.wait_ns))) {
+    if (!__syncthreads_and(mbar_wait(&sm.bar, parity, a.w.wait_ns))) {
         if (threadIdx.x == 0) atomicOr(a.w.err, 1u);
-        mbar_wait(&sm.bar, 0, a.w.wait_ns);
-        return;
+        mbar_wait(&sm.bar, parity, a.w.wait_ns);
+        return false;
     }
     const int ry0 = 4 * w;
     float2 ua[4], ub[4], cc[4], dd[4];   // ua = u(k0), ub = u(k0-1); then alternately overwritten
@@ -262,34 +282,57 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
         step(ua, ub, t);                           // u(k0+t) into ub
         if (t + 1 <= a.T) step(ub, ua, t + 1);     // u(k0+t+1) into ua
     }
+    return true;
 }
 
-// Issues the correlation slice of step t (u(kz0 - t), region rows 7 .. 8+TH) into u[t % 3].
-template <int WARPS>
-__device__ __forceinline__ void issue_u(AdjSmem<WARPS>& sm, const TileTma& tm, const TileAdj& a, int gl, int gx0,
-                                        int gy0, int t) {
-    uint64_t* bar = &sm.bar[1 + t % 3];
-    mbar_expect_tx(bar, Shape<WARPS>::USLICE_BYTES);
-    tma_load_3d(sm.u[t % 3], &tm.histu, gx0, gy0 + UOFF, gl * a.S + (a.kz0 - t) % a.S, bar);
-}
-// Parity of the u[t % 3] barrier phase that step t waits for (its (t-1)/3-th use).
-__device__ __forceinline__ uint32_t u_parity(int t) { return (uint32_t)((t - 1) / 3) & 1u; }
-
+// A launch computes one chunk (k_last = 0) or, persistent, the chunks k0+1 .. k_last one after
+// another with a grid barrier between them (every block resident: cooperative launch).
 template <int WARPS>
 __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
-    k_adj_tile(DevGeo g, const __grid_constant__ TileTma tm, TileAdj a, int tiles_x) {
+    k_fwd_tile(DevGeo g, const __grid_constant__ TileTma tm, TileFwd a0, int tiles_x) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    FwdSmem<WARPS>& sm = *reinterpret_cast<FwdSmem<WARPS>*>(smraw);
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    TileFwd a = a0;
+    for (unsigned int chunk = 0;; ++chunk) {
+        if (a0.k_last > 0) a.T = min(min(a0.k_last - a.k0, TMAXF), a0.S - 2);
+        if (!fwd_chunk<WARPS>(g, tm, a, tiles_x, smraw, chunk & 1u)) return;
+        a.k0 += a.T;
+        if (a0.k_last <= 0 || a.k0 >= a0.k_last) return;
+        if (!grid_sync(a0.w, chunk + 1)) return;
+    }
+}
+
+// Issues the correlation slice of step t (u(kz0 - t), region rows 7 .. 8+TH) into u[q % 3], q
+// the step's number since the launch began (its barrier is bar[1 + q % 3]).
+template <int WARPS>
+__device__ __forceinline__ void issue_u(AdjSmem<WARPS>& sm, const TileTma& tm, const TileAdj& a, int gl, int gx0,
+                                        int gy0, int t, int q) {
+    uint64_t* bar = &sm.bar[1 + q % 3];
+    mbar_expect_tx(bar, Shape<WARPS>::USLICE_BYTES);
+    tma_load_3d(sm.u[q % 3], &tm.histu, gx0, gy0 + UOFF, gl * a.S + (a.kz0 - t) % a.S, bar);
+}
+// Parity of the u[q % 3] barrier phase that launch step q waits for (its (q-1)/3-th use).
+__device__ __forceinline__ uint32_t u_parity(int q) { return (uint32_t)((q - 1) / 3) & 1u; }
+
+// One adjoint chunk of a block: z(kz0) .. z(kz0-T+1) with the correlation (the body of a
+// launch); the region barrier completes its phase `parity`, the launch's steps before this
+// chunk number q0.  False when a copy wait timed out.
+template <int WARPS>
+__device__ __forceinline__ bool adj_chunk(const DevGeo& g, const TileTma& tm, const TileAdj& a, int tiles_x,
+                                          unsigned char* smraw, uint32_t parity, int q0) {
     using S = Shape<WARPS>;
     constexpr int RH = S::RH, TH = S::TH;
-    extern __shared__ __align__(1024) unsigned char smraw[];
     AdjSmem<WARPS>& sm = *reinterpret_cast<AdjSmem<WARPS>*>(smraw);
     const int gl = blockIdx.y;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
     const int gx0 = tx * TW - HALO, gy0 = ty * TH - HALO;
     const int64_t N = (int64_t)g.nx * g.ny;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x < 4) mbar_init(&sm.bar[threadIdx.x], 1);
-    if (threadIdx.x == 0) mbar_fence_init();
-    __syncthreads();
     // residual rows of the launch's steps (z(m) injects rr[m]; row j holds m = kz0-T+1+j), loaded
     // while the copies fly
     float* const srr = reinterpret_cast<float*>(smraw + sizeof(AdjSmem<WARPS>));   // [T][nch]
@@ -306,8 +349,8 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
         tma_load_2d(sm.c, &tm.coef, gx0, gy0, &sm.bar[0]);
         tma_load_2d(sm.d, &tm.dmap, gx0, gy0, &sm.bar[0]);
         tma_load_2d(sm.rid, &tm.rid, gx0, gy0, &sm.bar[0]);
-        issue_u(sm, tm, a, gl, gx0, gy0, 1);
-        if (a.T >= 2) issue_u(sm, tm, a, gl, gx0, gy0, 2);
+        issue_u(sm, tm, a, gl, gx0, gy0, 1, q0 + 1);
+        if (a.T >= 2) issue_u(sm, tm, a, gl, gx0, gy0, 2, q0 + 2);
     }
     const int ry0 = 4 * w;
     const int ox = gx0 + 2 * lane;
@@ -319,10 +362,11 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
     const float2 zero = make_float2(0.f, 0.f);
 #pragma unroll
     for (int r = 0; r < 4; ++r) cr[r] = r < orows ? *reinterpret_cast<const float2*>(cbase + (int64_t)r * g.nx) : zero;
-    if (!__syncthreads_and(mbar_wait(&sm.bar[0], 0, a.w.wait_ns))) {
+    if (!__syncthreads_and(mbar_wait(&sm.bar[0], parity, a.w.wait_ns))) {
         if (threadIdx.x == 0) atomicOr(a.w.err, 1u);
-        for (int s = 1; s <= a.T && s <= 2; ++s) mbar_wait(&sm.bar[1 + s % 3], u_parity(s), a.w.wait_ns);
-        return;
+        for (int s = 1; s <= a.T && s <= 2; ++s)
+            mbar_wait(&sm.bar[1 + (q0 + s) % 3], u_parity(q0 + s), a.w.wait_ns);
+        return false;
     }
     // za = z(kz0+1), zb = z(kz0+2), pa = c z(kz0+1); then alternately overwritten
     float2 za[4], zb[4], cc[4], dd[4], pa[4], pb[4];
@@ -342,7 +386,7 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
     auto step = [&](float2 (&zc)[4], float2 (&zp)[4], float2 (&pc)[4], float2 (&pn)[4], int t) -> bool {
         const float* rrm = srr + (a.T - t) * g.nch;   // rr[m] of the slice computed, z(m), m = kz0-t+1
         // warp-uniform, so the shuffles below run with every lane of the warp
-        const bool ok = __all_sync(FULL, mbar_wait(&sm.bar[1 + t % 3], u_parity(t), a.w.wait_ns));
+        const bool ok = __all_sync(FULL, mbar_wait(&sm.bar[1 + (q0 + t) % 3], u_parity(q0 + t), a.w.wait_ns));
         // products c z(m+1) of the rows below and above the band
         float2 sb, nb;
         if (t == 1) {
@@ -372,7 +416,7 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
             }
             if (own_rows) {
                 // correlation with the Laplacian of u(m-1) (rows ry0-1 .. ry0+4 of the region)
-                const float* ub = sm.u[t % 3] + (ry0 - UOFF) * RX + 2 * lane;
+                const float* ub = sm.u[(q0 + t) % 3] + (ry0 - UOFF) * RX + 2 * lane;
                 float2 ur[6];
 #pragma unroll
                 for (int i = 0; i < 6; ++i) ur[i] = lds2(ub + (i - 1) * RX);
@@ -388,17 +432,18 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
         }
         if (!__syncthreads_and(ok)) {
             if (threadIdx.x == 0) atomicOr(a.w.err, 1u);
-            for (int s = t; s <= a.T && s <= t + 1; ++s) mbar_wait(&sm.bar[1 + s % 3], u_parity(s), a.w.wait_ns);
+            for (int s = t; s <= a.T && s <= t + 1; ++s)
+                mbar_wait(&sm.bar[1 + (q0 + s) % 3], u_parity(q0 + s), a.w.wait_ns);
             return false;
         }
-        // step t+2's slice into u[(t+2) % 3], last read by step t-1 (complete at the barrier above)
-        if (threadIdx.x == 0 && t + 2 <= a.T) issue_u(sm, tm, a, gl, gx0, gy0, t + 2);
+        // step t+2's slice into the ring slot last read by step t-1 (complete at the barrier above)
+        if (threadIdx.x == 0 && t + 2 <= a.T) issue_u(sm, tm, a, gl, gx0, gy0, t + 2, q0 + t + 2);
         return true;
     };
 #pragma unroll 1
     for (int t = 1; t <= a.T; t += 2) {
-        if (!step(za, zb, pa, pb, t)) return;                        // z(kz0-t+1) into zb
-        if (t + 1 <= a.T && !step(zb, za, pb, pa, t + 1)) return;    // z(kz0-t) into za
+        if (!step(za, zb, pa, pb, t)) return false;                        // z(kz0-t+1) into zb
+        if (t + 1 <= a.T && !step(zb, za, pb, pa, t + 1)) return false;    // z(kz0-t) into za
     }
     // z(kz0-T+1) and z(kz0-T+2) go to the ring (T = 1: only the first), with the correlation
     if (orows > 0) {
@@ -413,6 +458,33 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
             if (a.T > 1) *reinterpret_cast<float2*>(zbase + (int64_t)((mlast + 1) & 3) * N + o) = odd ? za[r] : zb[r];
             *reinterpret_cast<float2*>(cbase + o) = cr[r];
         }
+    }
+    return true;
+}
+
+// Adjoint steps of the next chunk when L steps remain: 6, 2 or 1 (the step counts whose output
+// slices miss the input slices' slots of the four-slot ring).
+__device__ __forceinline__ int adj_chunk_steps(int L) { return L >= 6 ? 6 : L >= 2 ? 2 : 1; }
+
+// A launch computes one chunk (kz_last = 0) or, persistent, z(kz0) .. z(kz_last) in chunks with
+// a grid barrier between them (every block resident: cooperative launch).
+template <int WARPS>
+__global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
+    k_adj_tile(DevGeo g, const __grid_constant__ TileTma tm, TileAdj a0, int tiles_x) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    AdjSmem<WARPS>& sm = *reinterpret_cast<AdjSmem<WARPS>*>(smraw);
+    if (threadIdx.x < 4) mbar_init(&sm.bar[threadIdx.x], 1);
+    if (threadIdx.x == 0) mbar_fence_init();
+    __syncthreads();
+    TileAdj a = a0;
+    int q0 = 0;
+    for (unsigned int chunk = 0;; ++chunk) {
+        if (a0.kz_last > 0) a.T = adj_chunk_steps(a.kz0 - a0.kz_last + 1);
+        if (!adj_chunk<WARPS>(g, tm, a, tiles_x, smraw, chunk & 1u, q0)) return;
+        q0 += a.T;
+        a.kz0 -= a.T;
+        if (a0.kz_last <= 0 || a.kz0 < a0.kz_last) return;
+        if (!grid_sync(a0.w, chunk + 1)) return;
     }
 }
 
@@ -509,7 +581,8 @@ void fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream
     // one fixed cap (the largest any launch asks for) rather than this launch's size: contexts on
     // other host threads launch the same kernel with other sizes
     cudaFuncSetAttribute(k_fwd_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem_cap<WARPS>());
-    launch_pdl(k_fwd_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
+    if (a.k_last > 0) launch_coop(k_fwd_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
+    else launch_pdl(k_fwd_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
 }
 template <int WARPS>
 void adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream) {
@@ -519,7 +592,27 @@ void adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream
     std::memcpy(&tm, m.raw[S::SET], sizeof tm);
     const size_t smem = sizeof(AdjSmem<WARPS>) + 4 * (size_t)a.T * g.nch;
     cudaFuncSetAttribute(k_adj_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_smem_cap<WARPS>());
-    launch_pdl(k_adj_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
+    if (a.kz_last > 0) launch_coop(k_adj_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
+    else launch_pdl(k_adj_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
+}
+
+// Blocks of a launch of `ng` groups against the blocks every SM can hold at once (at the fixed
+// shared-memory cap), for a persistent launch's grid barrier.
+template <int WARPS, bool FWD>
+bool persistent_fits(const DevGeo& g, int ng) {
+    using S = Shape<WARPS>;
+    const int tiles = ((g.nx + TW - 1) / TW) * ((g.ny + S::TH - 1) / S::TH) * ng;
+    auto kern = FWD ? reinterpret_cast<const void*>(k_fwd_tile<WARPS>) : reinterpret_cast<const void*>(k_adj_tile<WARPS>);
+    const size_t cap = FWD ? fwd_smem_cap<WARPS>() : adj_smem_cap<WARPS>();
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+    int per_sm = 0, dev = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::TPB, cap) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return tiles <= per_sm * sms;
 }
 }  // namespace
 
@@ -531,6 +624,11 @@ void launch_fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void*
 void launch_adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream) {
     if (a.warps == 10) adj_tile<10>(g, m, a, stream);
     else adj_tile<16>(g, m, a, stream);
+}
+
+bool tile_persistent_fits(const DevGeo& g, int warps, bool fwd, int ng) {
+    if (warps == 10) return fwd ? persistent_fits<10, true>(g, ng) : persistent_fits<10, false>(g, ng);
+    return fwd ? persistent_fits<16, true>(g, ng) : persistent_fits<16, false>(g, ng);
 }
 
 }  // namespace tomo
