@@ -28,9 +28,15 @@ def configs():
             for N in (64, 96, 128)]
 
 
-def test_batch_matches_sequential(built_lib):
+@pytest.mark.parametrize("form", ["graph", "threads"])
+def test_batch_matches_sequential(built_lib, form, monkeypatch):
+    """Both forms of the batch (one recorded graph per iteration; a host thread per context)."""
     import torch
 
+    if form == "threads":
+        monkeypatch.setenv("TOMO_BATCH_THREADS", "1")
+    else:
+        monkeypatch.delenv("TOMO_BATCH_THREADS", raising=False)
     dev = torch.device("cuda", 0)
     sched = tomo.schedule(omega=0.02, normalize=1)
     results = []
