@@ -91,6 +91,7 @@ struct tomo_ctx {
     int learned_resume = 0;      // plain steps after which paused proposals resume (0: never)
     static constexpr int ZR = 4; // adjoint ring slots
     TileMaps tmaps;              // TMA maps of hist, z, coef, dmap, rid (tile kernels)
+    TileMaps tmaps_ck;           // the same with the slice maps over the checkpoint buffer (pass_layout)
     unsigned int* err_host = nullptr;   // tile kernels' wait time-out word (mapped pinned memory)
     unsigned int* err_dev = nullptr;
     uint64_t wait_ns = 1000000000ull;   // bound of every tile-kernel copy wait (TOMO_WAIT_LIMIT_NS)
@@ -297,6 +298,11 @@ void encode_maps(tomo_ctx* c) {
         c->tile_fwd = c->tile_adj = c->tile_fwd1 = c->tile_adj1 = false;
         if (!why.empty() && std::getenv("TOMO_TUNE_LOG")) std::fprintf(stderr, "tomo: tile kernels off: %s\n", why.c_str());
     }
+    // short passes that keep their history in the checkpoint buffer read it through these
+    c->tmaps_ck.ok = false;
+    if (c->tmaps.ok && !c->full && c->ckpt)
+        encode_tile_maps(&c->tmaps_ck, c->dg, c->ckpt, (int64_t)c->P * c->nchunk * 2, c->z,
+                         (int64_t)c->P * tomo_ctx::ZR, c->coef, nullptr);
 }
 
 // Stream synchronisation that also reports a tile kernel's timed-out copy wait.
@@ -989,13 +995,18 @@ int64_t record_pass(tomo_ctx* c, int mode, int g0, int ng) {
 struct PassLayout {
     int S, K, nchunk;
     bool full;
+    bool in_ckpt;   // the pass's slices live in the checkpoint buffer (full history, no checkpoints)
 };
 PassLayout pass_layout(const tomo_ctx* c, int mode, int ng) {
-    const PassLayout plan{c->S, c->K, c->nchunk, c->full};
+    const PassLayout plan{c->S, c->K, c->nchunk, c->full, false};
     if (mode != MODE_GRAD || c->full || ng >= c->P || std::getenv("TOMO_FIXED_PASS_LAYOUT")) return plan;
     const int nt = c->geo.nt;
     const int64_t L = (int64_t)c->P * c->S / ng;
-    if (L >= nt) return PassLayout{nt, nt - 2, 1, true};
+    if (L >= nt) return PassLayout{nt, nt - 2, 1, true, false};
+    // a pass with full history needs no checkpoints: the checkpoint buffer (P nchunk 2 slices)
+    // holds the history when the slot buffer does not (tile kernels need its maps)
+    const bool ck_maps = !(ng == 1 ? c->tile_fwd1 || c->tile_adj1 : c->tile_fwd || c->tile_adj) || c->tmaps_ck.ok;
+    if ((int64_t)c->P * c->nchunk * 2 / ng >= nt && ck_maps) return PassLayout{nt, nt - 2, 1, true, true};
     int nchunk = (int)((nt - 2 + L - 2) / (L - 1));
     int K = (nt - 1 + nchunk - 1) / nchunk;
     if (K + 1 > L) {
@@ -1003,20 +1014,30 @@ PassLayout pass_layout(const tomo_ctx* c, int mode, int ng) {
         K = (nt - 1 + nchunk - 1) / nchunk;
     }
     if (K <= c->K) return plan;
-    return PassLayout{K + 1, K, (nt - 2 + K - 1) / K, false};
+    return PassLayout{K + 1, K, (nt - 2 + K - 1) / K, false, false};
 }
 
 // Applies a pass layout to the context while a pass is recorded, and restores the plan's.
 struct LayoutScope {
     tomo_ctx* c;
     PassLayout keep;
-    LayoutScope(tomo_ctx* ctx, const PassLayout& l) : c(ctx), keep{ctx->S, ctx->K, ctx->nchunk, ctx->full} {
+    bool swapped;
+    LayoutScope(tomo_ctx* ctx, const PassLayout& l)
+        : c(ctx), keep{ctx->S, ctx->K, ctx->nchunk, ctx->full, false}, swapped(l.in_ckpt) {
         c->S = l.S;
         c->K = l.K;
         c->nchunk = l.nchunk;
         c->full = l.full;
+        if (swapped) {
+            std::swap(c->hist, c->ckpt);
+            std::swap(c->tmaps, c->tmaps_ck);
+        }
     }
     ~LayoutScope() {
+        if (swapped) {
+            std::swap(c->hist, c->ckpt);
+            std::swap(c->tmaps, c->tmaps_ck);
+        }
         c->S = keep.S;
         c->K = keep.K;
         c->nchunk = keep.nchunk;
