@@ -333,7 +333,8 @@ def test_errors_are_status_codes():
 
 @pytest.mark.parametrize("adj_rows", ["1004", "1108", "1216", "232", "2008", "2032", "4008", "4132",
                                       "3204", "3308", "3332", "3416", "5232", "5316", "7008", "7016", "7108",
-                                      "8208", "8308", "8408", "8316", "9208", "9308", "9216", "9316"])
+                                      "8208", "8308", "8408", "8316", "9208", "9308", "9216", "9316",
+                                      "18208", "18308", "18408"])
 def test_two_step_adjoint_variants_match_one_step(adj_rows, monkeypatch):
     """The two-step adjoint's variants (interior fast path, inputs read ahead, four cells per
     lane, packed FP32x2 arithmetic, inputs staged in shared memory by cp.async) give the

@@ -460,11 +460,12 @@ tomo_status autotune(tomo_ctx* c) {
         for (int code : {rows, 100 + rows, 200 + rows, 1000 + rows, 1100 + rows, 1200 + rows, 2000 + rows,
                          4000 + rows, 4100 + rows, 3200 + rows, 3300 + rows, 3400 + rows, 5200 + rows,
                          5300 + rows, 7000 + rows, 7100 + rows, 8200 + rows, 8300 + rows, 8400 + rows,
-                         9200 + rows, 9300 + rows}) {
+                         9200 + rows, 9300 + rows, 18200 + rows, 18300 + rows, 18400 + rows}) {
+            if (code >= 18000 && rows != 8) continue;                 // packed unrolled staged: rows 8
             if (code >= 5000 && code < 7000 && rows < 16) continue;   // 8-block staged build: rows 16, 32
             if (code >= 7000 && code < 8000 && rows != 8 && rows != 16) continue;   // lean build: rows 8, 16
             if (code >= 8000 && code < 9000 && rows != 8 && code != 8316) continue;  // unrolled staged: rows 8 (16 at D 3)
-            if (code >= 9000 && rows != 8 && rows != 16) continue;   // four cells per lane, staged: rows 8, 16
+            if (code >= 9000 && code < 10000 && rows != 8 && rows != 16) continue;   // four cells per lane, staged: rows 8, 16
             if (rows < 4) break;
             float ms = 1e30f;
             for (int pass = 0; pass < passes; ++pass) {

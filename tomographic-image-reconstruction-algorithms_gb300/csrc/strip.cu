@@ -595,7 +595,9 @@ constexpr int ST_ROW = ST_ARR * 64;             // floats per staged row
 // MB: minimum resident blocks per SM for the register allocator (7: 72 registers; 8: 64, one
 // wave of C2's 1152 blocks, at the price of a few spilled values).
 // UNR: the row loop fully unrolled (ring slots and the receiver-bit shift become constants).
-template <int R, int D, int MB = 7, bool UNR = false>
+// PK: a lane's two cells in packed FP32x2 instructions (adj_cell2, lap5_2, pk_fma: the same
+// operation order and rounding, so the same bits, in fewer instructions).
+template <int R, int D, int MB = 7, bool UNR = false, bool PK = false>
 __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const float* __restrict__ coef, Adj2Step s) {
     extern __shared__ float4 st_mem4[];
     const int nx = g.nx, ny = g.ny;
@@ -689,7 +691,7 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
         const bool rcv = (rbits >> t) & 1ull;
         int2 rid = make_int2(-1, -1);
         if (rcv && ok) rid = *reinterpret_cast<const int2*>(g.rid + row + i);
-        const float2 pzp = mul2(cp, z1p);
+        const float2 pzp = PK ? pk_mul(cp, z1p) : mul2(cp, z1p);
         float2 za0 = make_float2(0.f, 0.f);
         {
             const float pw = __shfl_up_sync(FULL, pz0.y, 1), pe = __shfl_down_sync(FULL, pz0.x, 1);
@@ -706,11 +708,16 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
                     ix = rid.x >= 0 ? rra[rid.x] : 0.f;
                     iy = rid.y >= 0 ? rra[rid.y] : 0.f;
                 }
-                za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, ix, dx);
-                za0.y = adj_cell(pe, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, iy, dy);
+                if constexpr (PK) {
+                    za0 = adj_cell2(make_float2(pz0.y, pe), make_float2(pw, pz0.x), pzm, pzp, pz0, z10, zz,
+                                    make_float2(ix, iy), make_float2(dx, dy));
+                } else {
+                    za0.x = adj_cell(pz0.y, pw, pzm.x, pzp.x, pz0.x, z10.x, zz.x, ix, dx);
+                    za0.y = adj_cell(pe, pz0.x, pzm.y, pzp.y, pz0.y, z10.y, zz.y, iy, dy);
+                }
             }
         }
-        const float2 pa0 = mul2(c0, za0);
+        const float2 pa0 = PK ? pk_mul(c0, za0) : mul2(c0, za0);
         const int rb = r - 1;
         {
             const float pw = __shfl_up_sync(FULL, pam.y, 1), pe = __shfl_down_sync(FULL, pam.x, 1);
@@ -730,18 +737,26 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
                     ix = ridm.x >= 0 ? rrb[ridm.x] : 0.f;
                     iy = ridm.y >= 0 ? rrb[ridm.y] : 0.f;
                 }
-                float2 zbv;
-                zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, ix, dx);
-                zbv.y = adj_cell(pe, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, iy, dy);
-                const float lax = lap5(uam.y, uaw, uam2.x, ua0.x, uam.x);
-                const float lay = lap5(uae, uam.x, uam2.y, ua0.y, uam.y);
-                const float lbx = lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x);
-                const float lby = lap5(ube, ubm.x, ubm2.y, ub0.y, ubm.y);
-                float2 cr = crm;
-                cr.x = __fmaf_rn(zam.x, lax, cr.x);
-                cr.y = __fmaf_rn(zam.y, lay, cr.y);
-                cr.x = __fmaf_rn(zbv.x, lbx, cr.x);
-                cr.y = __fmaf_rn(zbv.y, lby, cr.y);
+                float2 zbv, cr = crm;
+                if constexpr (PK) {
+                    zbv = adj_cell2(make_float2(pam.y, pe), make_float2(pw, pam.x), pam2, pa0, pam, zam, z1m,
+                                    make_float2(ix, iy), make_float2(dx, dy));
+                    const float2 la = lap5_2(make_float2(uam.y, uae), make_float2(uaw, uam.x), uam2, ua0, uam);
+                    const float2 lb = lap5_2(make_float2(ubm.y, ube), make_float2(ubw, ubm.x), ubm2, ub0, ubm);
+                    cr = pk_fma(zam, la, cr);
+                    cr = pk_fma(zbv, lb, cr);
+                } else {
+                    zbv.x = adj_cell(pam.y, pw, pam2.x, pa0.x, pam.x, zam.x, z1m.x, ix, dx);
+                    zbv.y = adj_cell(pe, pam.x, pam2.y, pa0.y, pam.y, zam.y, z1m.y, iy, dy);
+                    const float lax = lap5(uam.y, uaw, uam2.x, ua0.x, uam.x);
+                    const float lay = lap5(uae, uam.x, uam2.y, ua0.y, uam.y);
+                    const float lbx = lap5(ubm.y, ubw, ubm2.x, ub0.x, ubm.x);
+                    const float lby = lap5(ube, ubm.x, ubm2.y, ub0.y, ubm.y);
+                    cr.x = __fmaf_rn(zam.x, lax, cr.x);
+                    cr.y = __fmaf_rn(zam.y, lay, cr.y);
+                    cr.x = __fmaf_rn(zbv.x, lbx, cr.x);
+                    cr.y = __fmaf_rn(zbv.y, lby, cr.y);
+                }
                 *reinterpret_cast<float2*>(corr + rowb + i) = cr;
                 *reinterpret_cast<float2*>(za + rowb + i) = zam;
                 *reinterpret_cast<float2*>(zb + rowb + i) = zbv;
@@ -761,12 +776,12 @@ __global__ void __launch_bounds__(WARPS * 32, MB) k_adj2s_strip(DevGeo g, const 
     cp_async_wait<0>();                                  // nothing left in flight at exit
 }
 
-template <int R, int D, int MB = 7, bool UNR = false>
+template <int R, int D, int MB = 7, bool UNR = false, bool PK = false>
 void adj2s_strip(const DevGeo& g, const float* coef, const Adj2Step& s, cudaStream_t st) {
     const int rows_per_block = WARPS * R;
     const size_t smem = sizeof(float) * WARPS * D * ST_ROW;
     dim3 grid((g.nx + 2 + 59) / 60, (g.ny + rows_per_block - 1) / rows_per_block, s.ng);
-    k_adj2s_strip<R, D, MB, UNR><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
+    k_adj2s_strip<R, D, MB, UNR, PK><<<grid, WARPS * 32, smem, st>>>(g, coef, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1749,6 +1764,9 @@ void launch_adj2_strip(int rows, const DevGeo& g, const float* coef, const AdjSt
     case 8308: adj2s_strip<8, 3, 6, true>(g, coef, s, st); return;
     case 8408: adj2s_strip<8, 4, 6, true>(g, coef, s, st); return;
     case 8316: adj2s_strip<16, 3, 6, true>(g, coef, s, st); return;
+    case 18208: adj2s_strip<8, 2, 5, true, true>(g, coef, s, st); return;   // 10000 + unrolled staged: packed FP32x2, 5 blocks
+    case 18308: adj2s_strip<8, 3, 5, true, true>(g, coef, s, st); return;
+    case 18408: adj2s_strip<8, 4, 5, true, true>(g, coef, s, st); return;
     case 5216: adj2s_strip<16, 2, 8>(g, coef, s, st); return;   // 5000 + 100 D + rows: staged, 8 blocks
     case 5232: adj2s_strip<32, 2, 8>(g, coef, s, st); return;
     case 5316: adj2s_strip<16, 3, 8>(g, coef, s, st); return;
