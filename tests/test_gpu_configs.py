@@ -99,6 +99,9 @@ KERNELS = {
                             TOMO_ADJ_PAIR_ROWS="3308", TOMO_TILE="0"),
     "fwd6008-adj7016": dict(TOMO_STRIP_ROWS="8", TOMO_FWD_ROWS="6008", TOMO_FWD_PAIR="0", TOMO_ADJ_PAIR="1",
                             TOMO_ADJ_PAIR_ROWS="7016", TOMO_TILE="0"),
+    # prefetching lean forward and the packed staged two-step adjoint
+    "fwd6108-adj18408": dict(TOMO_STRIP_ROWS="8", TOMO_FWD_ROWS="6108", TOMO_FWD_PAIR="0", TOMO_ADJ_PAIR="1",
+                             TOMO_ADJ_PAIR_ROWS="18408", TOMO_TILE="0"),
     "tiles": dict(TOMO_STRIP_ROWS="8", TOMO_FWD_PAIR="0", TOMO_ADJ_PAIR="0", TOMO_TILE="1"),
 }
 

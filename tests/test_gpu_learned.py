@@ -250,3 +250,48 @@ def test_shipped_network_gain(torch_dev):
         eps, kind, sweeps, _ = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), target, 30)
         assert eps[-1] <= target, (list(eps), target)
         assert sweeps <= 15, (sweeps, list(eps), list(kind))
+
+
+# Phantom seeds of the time-to-image evaluation: none was among the training phantoms; 3001-3005
+# chose the acceptance rule, the other fifteen were used for nothing before it was fixed.
+HELD_OUT_SEEDS = tuple(range(2001, 2006)) + tuple(range(3001, 3006)) + tuple(range(4001, 4006)) + \
+    tuple(range(5001, 5006))
+
+
+def test_shipped_network_gain_on_held_out_phantoms(torch_dev):
+    """Time to image over 20 held-out phantoms of the 512x512 workload (ellipse axes 10-60
+    cells, 1 % record noise): plain weighted SIRT runs 30 iterations from f = 0; the learned
+    update (default acceptance rule) runs from f = 0 until its image error is at or below plain's
+    final one.  Every phantom must get there, and the geometric mean of the sweep ratio
+    30 / learned sweeps (the wall-time ratio: a sweep is one forward plus one adjoint solve of all
+    32 groups and dominates both loops) must be at least 3."""
+    import os
+
+    torch, dev = torch_dev
+    cfg = tomo.cfg_config(nx=512, ny=512, nt=2500, n_transducers=256, group_size=8, radius=220.0,
+                          ckpt_interval=50)
+    sched = tomo.schedule(omega=0.02, normalize=1)
+    net = tomo.Net(0)
+    net.load(os.path.join(tomo.PKG_DIR, "weights", "learned_update.bin"))
+    rows = []
+    with tomo.Context(cfg) as ctx:
+        d_f = torch.zeros((512, 512), dtype=torch.float32, device=dev)
+        for seed in HELD_OUT_SEEDS:
+            fo = tomo.phantom_cfg(512, 512, 1, 8, 10.0, 60.0, 0.15, 0.01, 0.8 * cfg.radius, seed)
+            ctx.set_records(ctx.generate_data(fo, noise_level=0.01, seed=77))
+            d_ft = torch.from_numpy(fo).to(dev)
+            d_f.zero_()
+            torch.cuda.synchronize(dev)
+            for it in range(30):
+                st = ctx.iterate_device(tomo.SIRT_NORM, sched, it, d_f.data_ptr(), 0, d_ft.data_ptr())
+            target = st.epsilon
+            d_f.zero_()
+            torch.cuda.synchronize(dev)
+            eps, kind, sweeps, _ = ctx.run_learned(net, sched, d_f.data_ptr(), d_ft.data_ptr(), target, 90)
+            steps = "".join({1: "L", 2: "l", 0: "x", -1: "p"}[int(k)] for k in kind)
+            rows.append((seed, target, float(eps[-1]), sweeps, steps))
+    table = "; ".join(f"{s}: {sw} sweeps {st} eps {e:.2f}/{t:.2f} %" for s, t, e, sw, st in rows)
+    assert all(e <= t for _, t, e, _, _ in rows), table
+    ratios = np.array([30.0 / sw for _, _, _, sw, _ in rows])
+    gmean = float(np.exp(np.mean(np.log(ratios))))
+    assert gmean >= 3.0, f"geometric mean {gmean:.2f}x ({table})"
