@@ -77,6 +77,18 @@ static_assert(sizeof(TileTma) == sizeof(TileMaps::raw[0]), "tensor map size");
 
 __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+
+// Record rows (T steps x nch channels) into shared memory by asynchronous 4-byte copies: a
+// thread's copies are all in flight at once, where a load-then-store loop through generic
+// pointers waits out one memory latency per element it copies.  The caller completes them with
+// cp_async_wait_all() before the barrier that publishes the region.
+__device__ __forceinline__ void copy_rows_async(float* dst, const float* src, int n, int tid, int nthreads) {
+    for (int i = tid; i < n; i += nthreads)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst + i)),
+                     "l"(__cvta_generic_to_global(src + i))
+                     : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 #include "async.cuh"
 
 // Forward cell update of a lane's two cells (fwd_cell of cell.cuh, packed).
@@ -178,10 +190,8 @@ __device__ __forceinline__ bool fwd_chunk(const DevGeo& g, const TileTma& tm, co
         const int k = a.k0 + threadIdx.x;          // step threadIdx.x + 1 computes slice k + 1
         ssrc[threadIdx.x] = (int)threadIdx.x < a.T && k < g.n_src_steps ? g.src[k] : 0.f;
     }
-    if (a.gmeas) {   // measured records: set before the passes, written by no kernel
-        const float* gm = a.gmeas + ((int64_t)gl * g.nt + a.k0 + 1) * g.nch;
-        for (int i = threadIdx.x; i < a.T * g.nch; i += S::TPB) smeas[i] = gm[i];
-    }
+    if (a.gmeas)     // measured records: set before the passes, written by no kernel
+        copy_rows_async(smeas, a.gmeas + ((int64_t)gl * g.nt + a.k0 + 1) * g.nch, a.T * g.nch, threadIdx.x, S::TPB);
     grid_dep_wait();
     grid_dep_trigger();
     if (threadIdx.x == 0) {
@@ -192,6 +202,7 @@ __device__ __forceinline__ bool fwd_chunk(const DevGeo& g, const TileTma& tm, co
         tma_load_2d(sm.d, &tm.dmap, gx0, gy0, &sm.bar);
         tma_load_2d(sm.rid, &tm.rid, gx0, gy0, &sm.bar);
     }
+    cp_async_wait_all();                           // this thread's record-row copies
     if (!__syncthreads_and(mbar_wait(&sm.bar, parity, a.w.wait_ns))) {
         if (threadIdx.x == 0) atomicOr(a.w.err, 1u);
         mbar_wait(&sm.bar, parity, a.w.wait_ns);
@@ -338,10 +349,7 @@ __device__ __forceinline__ bool adj_chunk(const DevGeo& g, const TileTma& tm, co
     float* const srr = reinterpret_cast<float*>(smraw + sizeof(AdjSmem<WARPS>));   // [T][nch]
     grid_dep_wait();
     grid_dep_trigger();
-    {
-        const float* rg = a.rr + gl * a.rrstride + (int64_t)(a.kz0 - a.T + 1) * g.nch;
-        for (int i = threadIdx.x; i < a.T * g.nch; i += S::TPB) srr[i] = rg[i];
-    }
+    copy_rows_async(srr, a.rr + gl * a.rrstride + (int64_t)(a.kz0 - a.T + 1) * g.nch, a.T * g.nch, threadIdx.x, S::TPB);
     if (threadIdx.x == 0) {
         mbar_expect_tx(&sm.bar[0], S::REGION_BYTES + a.w.extra_tx);
         tma_load_3d(sm.z1, &tm.z, gx0, gy0, gl * 4 + ((a.kz0 + 1) & 3), &sm.bar[0]);
@@ -362,6 +370,7 @@ __device__ __forceinline__ bool adj_chunk(const DevGeo& g, const TileTma& tm, co
     const float2 zero = make_float2(0.f, 0.f);
 #pragma unroll
     for (int r = 0; r < 4; ++r) cr[r] = r < orows ? *reinterpret_cast<const float2*>(cbase + (int64_t)r * g.nx) : zero;
+    cp_async_wait_all();                           // this thread's residual-row copies
     if (!__syncthreads_and(mbar_wait(&sm.bar[0], parity, a.w.wait_ns))) {
         if (threadIdx.x == 0) atomicOr(a.w.err, 1u);
         for (int s = 1; s <= a.T && s <= 2; ++s)
