@@ -180,7 +180,7 @@ def run_batch(args, local, rank, world, dist):
     h2d = sum(4 * (fo.size + r.numel()) for fo, r in zip(fos, recs))
     if rank == 0:
         line = {
-            "metric": metric_name(), "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "metric": metric_name(args.workload), "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded ellipse phantoms + smoothed noise, 1% Gaussian record noise)",
@@ -328,7 +328,7 @@ def reference_arm(args, w, rank, world):
     dt = sum(ts)
     gbs = cu * args.steps / 2 * 36.0 / dt / 1e9
     line = {
-        "impl": "reference", "metric": metric_name(), "value": gbs, "unit": "GB/s", "n_gpus": world,
+        "impl": "reference", "metric": metric_name(args.workload), "value": gbs, "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded phantom)", "config": {"workload": args.workload + ": " + w["desc"]},
@@ -340,8 +340,11 @@ def reference_arm(args, w, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def metric_name():
-    return "stencil GB/s (algorithmic 36 B per forward+adjoint cell-update) of one plain weighted SIRT iteration"
+def metric_name(workload="c2"):
+    """The metric of a workload's line (both arms print the same string for the same workload)."""
+    what = {"c1": "one plain uniform SIRT iteration", "c3": "one batched plain weighted SIRT iteration",
+            "ref192": "one normalised SIRT iteration"}.get(workload, "one plain weighted SIRT iteration")
+    return "stencil GB/s (algorithmic 36 B per forward+adjoint cell-update) of " + what
 
 
 WEIGHTS = os.path.join(PKG, "weights", "learned_update.bin")
@@ -625,7 +628,7 @@ def main():
 
     if rank == 0:
         line = {
-            "metric": metric_name(), "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "metric": metric_name(args.workload), "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded ellipse phantom + smoothed noise, 1% Gaussian record noise)",

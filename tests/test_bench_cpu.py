@@ -38,6 +38,7 @@ def test_reference_arm_line():
     assert d["value"] > 0 and d["ms_per_step"] > 0
     assert d["higher_is_better"] is True
     assert d["config"]["workload"].startswith("c1")
+    assert d["metric"].endswith("of one plain uniform SIRT iteration")   # C1's update rule
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     assert cb["value"] == d["value"] and cb["unit"] == d["unit"]
