@@ -33,7 +33,14 @@ def phantom(cfg, seed):
     return tomo.phantom_cfg(cfg.nx, cfg.ny, 0, 3, 4, 9, 0.1, 0.0, 28.0, seed)
 
 
-def test_fixed_noise_residual_matches_restatement(built_lib):
+@pytest.mark.parametrize("kernels", ["tuned", "tiles"])
+def test_fixed_noise_residual_matches_restatement(built_lib, kernels, monkeypatch):
+    """The residual under fixed noise against the numpy restatement of the draw, through the
+    kernels the tuner picks and through the multi-step tile kernels (whose forward has a
+    separate instantiation for noisy launches)."""
+    if kernels == "tiles":
+        monkeypatch.setenv("TOMO_TILE", "1")
+        monkeypatch.setenv("TOMO_STRIP_ROWS", "8")
     cfg = cfg_small()
     fo = phantom(cfg, 3)
     f0 = np.zeros_like(fo)

@@ -169,8 +169,12 @@ __device__ __forceinline__ bool grid_sync(const TileWait& w, unsigned int chunk)
 }
 
 // One forward chunk of a block: slices k0+1 .. k0+T of its tile (the body of a launch); the
-// region barrier completes its phase `parity`.  False when a copy wait timed out.
-template <int WARPS>
+// region barrier completes its phase `parity`.  False when a copy wait timed out.  NOISY: the
+// launch applies in-loop record noise.  A separate instantiation keeps the noise draw out of
+// the noise-free kernel entirely: as a run-time select inside the receiver branch, the draw (a
+// 64-bit hash) was evaluated for every receiver cell every step and held up the warps on the
+// transducer circle (1.4 ms of a 6.7 ms one-group pass on 512x512 with 256 receivers).
+template <int WARPS, bool NOISY>
 __device__ __forceinline__ bool fwd_chunk(const DevGeo& g, const TileTma& tm, const TileFwd& a, int tiles_x,
                                           unsigned char* smraw, uint32_t parity) {
     using S = Shape<WARPS>;
@@ -224,7 +228,7 @@ __device__ __forceinline__ bool fwd_chunk(const DevGeo& g, const TileTma& tm, co
     const int ox = gx0 + 2 * lane;
     const bool own = w >= HALO / 4 && w < WARPS - HALO / 4 && lane >= HALO / 2 && lane < (HALO + TW) / 2 && ox < g.nx;
     if (!own) rmask = 0u;
-    const bool noisy = a.gmeas && g.noise_key;
+    const bool noisy = NOISY && a.gmeas && g.noise_key;
     const uint64_t key = noisy ? *g.noise_key : 0;
     float* const obase = a.hist + gl * a.gstride + (int64_t)(gy0 + ry0) * g.nx + ox;   // owned row 0 of slot 0
     float* const cbase = a.ckpt ? a.ckpt + gl * a.ckstride + (int64_t)(gy0 + ry0) * g.nx + ox : nullptr;
@@ -298,7 +302,7 @@ __device__ __forceinline__ bool fwd_chunk(const DevGeo& g, const TileTma& tm, co
 
 // A launch computes one chunk (k_last = 0) or, persistent, the chunks k0+1 .. k_last one after
 // another with a grid barrier between them (every block resident: cooperative launch).
-template <int WARPS>
+template <int WARPS, bool NOISY>
 __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
     k_fwd_tile(DevGeo g, const __grid_constant__ TileTma tm, TileFwd a0, int tiles_x) {
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -311,7 +315,7 @@ __global__ void __launch_bounds__(Shape<WARPS>::TPB, Shape<WARPS>::MINB)
     TileFwd a = a0;
     for (unsigned int chunk = 0;; ++chunk) {
         if (a0.k_last > 0) a.T = min(min(a0.k_last - a.k0, TMAXF), a0.S - 2);
-        if (!fwd_chunk<WARPS>(g, tm, a, tiles_x, smraw, chunk & 1u)) return;
+        if (!fwd_chunk<WARPS, NOISY>(g, tm, a, tiles_x, smraw, chunk & 1u)) return;
         a.k0 += a.T;
         if (a0.k_last <= 0 || a.k0 >= a0.k_last) return;
         if (!grid_sync(a0.w, chunk + 1)) return;
@@ -589,9 +593,10 @@ void fwd_tile(const DevGeo& g, const TileMaps& m, const TileFwd& a, void* stream
     const size_t smem = sizeof(FwdSmem<WARPS>) + 4 * (TMAXF + (a.gmeas ? (size_t)a.T * g.nch : 0));
     // one fixed cap (the largest any launch asks for) rather than this launch's size: contexts on
     // other host threads launch the same kernel with other sizes
-    cudaFuncSetAttribute(k_fwd_tile<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem_cap<WARPS>());
-    if (a.k_last > 0) launch_coop(k_fwd_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
-    else launch_pdl(k_fwd_tile<WARPS>, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
+    const auto kern = a.gmeas && g.noise_key ? k_fwd_tile<WARPS, true> : k_fwd_tile<WARPS, false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem_cap<WARPS>());
+    if (a.k_last > 0) launch_coop(kern, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
+    else launch_pdl(kern, dim3(tiles_x * tiles_y, a.ng), S::TPB, smem, stream, g, tm, a, tiles_x);
 }
 template <int WARPS>
 void adj_tile(const DevGeo& g, const TileMaps& m, const TileAdj& a, void* stream) {
@@ -611,17 +616,26 @@ template <int WARPS, bool FWD>
 bool persistent_fits(const DevGeo& g, int ng) {
     using S = Shape<WARPS>;
     const int tiles = ((g.nx + TW - 1) / TW) * ((g.ny + S::TH - 1) / S::TH) * ng;
-    auto kern = FWD ? reinterpret_cast<const void*>(k_fwd_tile<WARPS>) : reinterpret_cast<const void*>(k_adj_tile<WARPS>);
     const size_t cap = FWD ? fwd_smem_cap<WARPS>() : adj_smem_cap<WARPS>();
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
-    int per_sm = 0, dev = 0, sms = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::TPB, cap) != cudaSuccess ||
-        cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    // every instantiation a launch may use (the forward's noise-free and noisy forms)
+    const void* kerns[2] = {
+        FWD ? reinterpret_cast<const void*>(k_fwd_tile<WARPS, false>) : reinterpret_cast<const void*>(k_adj_tile<WARPS>),
+        FWD ? reinterpret_cast<const void*>(k_fwd_tile<WARPS, true>) : reinterpret_cast<const void*>(k_adj_tile<WARPS>)};
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return tiles <= per_sm * sms;
+    for (const void* kern : kerns) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::TPB, cap) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (tiles > per_sm * sms) return false;
+    }
+    return true;
 }
 }  // namespace
 
