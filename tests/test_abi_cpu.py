@@ -255,3 +255,11 @@ def test_cli_generate_field_binary(built_lib, tmp_path):
     dims, vals = read_bin(tmp_path / "fo.bin")
     assert list(dims) == [192, 192, 1, 1]
     assert np.array_equal(vals.reshape(192, 192), O.phantom_ref())
+
+
+def test_net_parameter_count_matches_oracle_layout(built_lib):
+    """The network's flat parameter vector has the oracle's layout size (first layer stored with
+    its 3 feature channels zero-padded to 16), so weights move between the two unchanged."""
+    import cnn_oracle as K
+
+    assert tomo.lib().tomo_net_num_params() == K.N_PARAMS == sum(int(np.prod(s)) for _, s in K.SHAPES)
