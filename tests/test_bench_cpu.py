@@ -1,4 +1,4 @@
-"""The benchmark's command-line contract, checked on a machine without a GPU.
+"""The benchmark's command-line contract and host logic, checked on a machine without a GPU.
 
 * The reference arm (``--impl reference``: the oracle's FP32 transcription of the reference
   kernels on the host cores) prints one JSON line with the keys a reader of the benchmark
@@ -45,6 +45,25 @@ def test_reference_arm_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_clock_summary_of_samples():
+    """The clocks record of the timed region: median SM clock, the largest maximum clock and the
+    throttle reasons seen active in any sample (nvidia-smi's csv, noheader, nounits form); no
+    samples reads as unsampled."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    s = bench.ClockSampler(0)                 # not entered: nothing runs nvidia-smi
+    s.tmp.write("0, 2070, 2070, 900.50, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n"
+                "0, 2055, 2070, 1391.2, 0x0000000000000004, Not Active, Not Active, Not Active, Active\n"
+                "0, 2070, 2070, 1100.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n")
+    d = s.summary()
+    assert d == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    s = bench.ClockSampler(0)
+    s.tmp.write("0, 1200, 2070, 700.0, 0x0000000000000040, Not Active, Active, Not Active, Not Active\n")
+    assert s.summary()["reasons"] == ["hw_thermal_slowdown"]
+    assert bench.ClockSampler(0).summary()["reasons"] == ["unsampled"]
 
 
 def test_gpu_arm_needs_a_gpu():
