@@ -5,6 +5,8 @@
   parses: the metric and its unit, the step and warm-up counts, ``cpu_baseline`` describing the
   run and an ``e2e`` block whose value is the line's own with no host-device traffic.
 * The GPU arm has no CPU path: without a CUDA device it exits non-zero and prints no line.
+* The clocks record of the timed region is summarised from nvidia-smi samples as the timing
+  rules read it (median SM clock, throttle reasons seen active).
 """
 import json
 import os
