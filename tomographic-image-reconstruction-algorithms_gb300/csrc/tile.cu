@@ -173,7 +173,7 @@ __device__ __forceinline__ bool grid_sync(const TileWait& w, unsigned int chunk)
 // launch applies in-loop record noise.  A separate instantiation keeps the noise draw out of
 // the noise-free kernel entirely: as a run-time select inside the receiver branch, the draw (a
 // 64-bit hash) was evaluated for every receiver cell every step and held up the warps on the
-// transducer circle (1.4 ms of a 6.7 ms one-group pass on 512x512 with 256 receivers).
+// transducer circle (0.36 ms of a 6.7 ms one-group pass on 512x512 with 256 receivers).
 template <int WARPS, bool NOISY>
 __device__ __forceinline__ bool fwd_chunk(const DevGeo& g, const TileTma& tm, const TileFwd& a, int tiles_x,
                                           unsigned char* smraw, uint32_t parity) {
